@@ -1,0 +1,368 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 2D Euler step: cell-updates/s of SSP-RK3 steps.
+
+Workload (default): the 4096 x 4096 four-quadrant Riemann problem (seeded
+rho, p ~ U[0.1, 2], u, v ~ U[-1, 1] per quadrant, gamma = 1.4, 3 ghost cells,
+transmissive boundaries), characteristic WENO5 + 2-point Gauss-quadrature faces
++ HLLE, CFL 0.45, FP64.  One step = one full SSP-RK3 step (three residual
+evaluations, stage combinations, boundary fills and the CFL reduction) over
+all nx*ny cells; one cell-update = one cell advanced one step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+gb300 arm: the device-resident solver (weno_ext.Solver, C ABI of
+libweno_gb300.so) with the state resident in HBM; `value` is whole-job
+cell-updates/s over the K timed steps (CUDA events on the solver's stream,
+barrier + synchronize on both sides, max over ranks).  `e2e` is the same metric
+through the public API with host buffers: every step copies the (nx+6, ny+6, 8)
+state in from pinned host memory and the result back.  Under torchrun each rank
+runs an independent replica (the path does not shard here).
+
+reference arm: the reference's CPU implementation of the path -- the oracle's
+C++ restatement of the Rust core and driver step (the Rust crate cannot be
+built without a Rust toolchain) -- on all host cores, on a bounded strip of
+the same workload per step.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "weno-cfd-solver_gb300")
+for _p in (ROOT, PKG, os.path.join(ROOT, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+GAMMA = 1.4
+SEED = 20261203
+METRIC = "cell-updates/s (4096^2 four-quadrant Riemann, char-WENO5+GQ+HLLE, SSP-RK3, FP64)"
+UNIT = "cell-updates/s"
+# Kernel classes reported by weno_solver_timing_report.
+CLASSES = ["cfl+dt", "bc", "pass1_x", "pass2_x", "blend", "pass1_y", "pass2_y", "residual+rk"]
+
+
+def quadrant_state(nx, ny, seed=SEED):
+    from states import quadrant
+    return quadrant(np.random.default_rng(seed), nx, ny)
+
+
+def load_json(path):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names[1:], parts[5:9]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(nx, strip_ny, threads, seconds_hint=15.0):
+    """The oracle (C++ restatement of the Rust core and driver step) timed on host
+    cores over a strip of the workload: nx x strip_ny interior cells."""
+    from oracle import oracle
+    used = oracle.set_threads(threads)
+    q = quadrant_state(nx, strip_ny, seed=SEED + 1)
+    oracle.bc_transmissive(q)
+    dx = 1.0 / nx
+    dt = 0.45 * dx / oracle.cfl_cmax(q, nx, strip_ny, GAMMA)
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        oracle.rk3_step(q, nx, strip_ny, dx, dt, GAMMA, True, (0.2, 1.0), False)
+        steps += 1
+        if time.perf_counter() - t0 >= seconds_hint or steps >= 50:
+            break
+    el = time.perf_counter() - t0
+    return {"value": nx * strip_ny * steps / el, "unit": UNIT, "cores": used, "kind": "port",
+            "sample": f"{steps} SSP-RK3 step(s) of a {nx} x {strip_ny} strip of the same workload "
+                      f"(oracle C++ restatement, OpenMP, {used} threads), {el:.1f} s"}
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    nx = args.nx
+    # Bounded sample: a strip of the workload sized for a few seconds per step.
+    strip = int(os.environ.get("WENO_REF_STRIP", "48"))
+    from oracle import oracle
+    used = oracle.set_threads(nthreads)
+    q = quadrant_state(nx, strip, seed=SEED + 1)
+    oracle.bc_transmissive(q)
+    dx = 1.0 / nx
+    for _ in range(args.warmup):
+        dt = 0.45 * dx / oracle.cfl_cmax(q, nx, strip, GAMMA)
+        oracle.rk3_step(q, nx, strip, dx, dt, GAMMA, True, (0.2, 1.0), False)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dt = 0.45 * dx / oracle.cfl_cmax(q, nx, strip, GAMMA)
+        oracle.rk3_step(q, nx, strip, dx, dt, GAMMA, True, (0.2, 1.0), False)
+    el = time.perf_counter() - t0
+    value = nx * strip * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"four-quadrant Riemann {nx}x{args.ny} (timed on a {nx}x{strip} strip per step), "
+                               "char-WENO5+GQ+HLLE, SSP-RK3, CFL 0.45", "nx": nx, "ny": args.ny,
+                   "sample_ny": strip},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": "port",
+                         "sample": f"{args.steps} step(s) of a {nx} x {strip} strip, oracle C++ restatement of "
+                                   f"the Rust core (Rust toolchain absent), OpenMP {used} threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def time_solver(Solver, q0, nx, ny, steps, warmup, **kw):
+    """Device-resident run; returns (ms for `steps` timed steps, solver)."""
+    import torch
+    s = Solver(nx, ny, 1.0 / nx, GAMMA, **kw)
+    s.set_state(q0)
+    s.run(warmup, graph=True)
+    s.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s.stream)
+    s.run(steps, graph=True)
+    e1.record(s.stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1), s
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nx", type=int, default=4096)
+    ap.add_argument("--ny", type=int, default=4096)
+    ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    import weno_ext
+    from weno_ext import _lib
+    L = _lib.load()
+
+    nx, ny = args.nx, args.ny
+    q0 = quadrant_state(nx, ny)
+    kw = dict(precision=64, mode=args.mode, cons=False, force_hlle=True, jp_cri=(0.2, 1.0), cfl=0.45)
+    s = weno_ext.Solver(nx, ny, 1.0 / nx, GAMMA, **kw)
+    s.set_state(q0)
+    s.run(args.warmup, graph=False)
+    s.synchronize()
+
+    # ---- timed region: K steps, per-kernel-class events on the solver stream ----
+    import ctypes
+    _lib.check(L.weno_solver_enable_timing(s._h, 1), "timing")
+    clocks = ClockSampler(torch.cuda.current_device())
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s.stream)
+    s.run(args.steps, graph=False)
+    e1.record(s.stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_cls = (ctypes.c_double * len(CLASSES))()
+    n_cls = (ctypes.c_int64 * len(CLASSES))()
+    _lib.check(L.weno_solver_timing_report(s._h, ms_cls, n_cls, len(CLASSES)), "timing report")
+    _lib.check(L.weno_solver_enable_timing(s._h, 0), "timing")
+    t_sim, nsteps_done, status = s.info()
+    launches = s.launches_per_step * args.steps
+    value = nx * ny * args.steps * world / (ms / 1e3)
+
+    # ---- dominant kernel and its roofline ----
+    kern = {CLASSES[i]: {"ms": ms_cls[i], "launches": int(n_cls[i])} for i in range(len(CLASSES)) if n_cls[i]}
+    dom = max(kern, key=lambda k: kern[k]["ms"])
+    M, N = nx + 6, ny + 6
+    es = 8
+    # Algorithmic bytes per launch: the stencil input once plus the outputs once.
+    alg_bytes = {
+        "pass1_x": (4 * M * N + 8 * (M - 5) * N) * es,
+        "pass1_y": (4 * M * N + 8 * M * (N - 5)) * es,
+        "pass2_x": (8 * (M - 5) * N + 4 * (M - 5) * (N - 6)) * es,
+        "pass2_y": (8 * M * (N - 5) + 4 * (M - 6) * (N - 5)) * es,
+        "residual+rk": (8 * (M - 5) * (N - 6) // 2 + 4 * (M - 6) * (N - 5) + 12 * nx * ny) * es,
+    }
+    peaks = load_json(os.path.join(ROOT, "MEASURED_PEAKS.json")) or {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    per_launch_ms = kern[dom]["ms"] / max(kern[dom]["launches"], 1)
+    achieved = alg_bytes.get(dom, 0) / (per_launch_ms / 1e3) / 1e9 if dom in alg_bytes else None
+    prof = load_json(os.path.join(ROOT, "profiles", "roofline_traffic.json")) or {}
+    traffic = prof.get(dom, {}).get("dram_bytes_per_launch") if isinstance(prof.get(dom), dict) else None
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"}
+    r64, rdiv, r32 = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    _lib.check(L.weno_probe_rates(ctypes.byref(r64), ctypes.byref(rdiv), ctypes.byref(r32), None), "probe")
+    flops = load_json(os.path.join(ROOT, "profiles", "flops_per_cell.json")) or {}
+    fpc = flops.get("char_hlle_step")
+    compute = None
+    if fpc and r64.value > 0:
+        ach = fpc * value / world / 1e12
+        compute = {"bound": "fp64", "achieved": ach, "peak": r64.value, "unit": "TFLOP/s",
+                   "frac": ach / r64.value, "flops_per_cell_update": fpc,
+                   "measured_rates": {"fp64_fma_tflops": r64.value, "fp64_div_per_s": rdiv.value,
+                                      "fp32_fma_tflops": r32.value},
+                   "note": "algorithmic FLOPs of the reference algorithm per cell-update (oracle tally: add, mul, "
+                           "div and sqrt count 1 each); peak = FP64 FMA rate measured live on this GPU"}
+
+    # ---- e2e: public API with host buffers, H2D + D2H every step ----
+    host = torch.empty((M, N, 8), dtype=torch.float64).pin_memory()
+    host.numpy()[:] = q0
+    hp = host.data_ptr()
+    s2 = weno_ext.Solver(nx, ny, 1.0 / nx, GAMMA, **kw)
+    L.weno_solver_set_state_host(s2._h, hp, 8)
+    s2.run(1, graph=True)
+    L.weno_solver_get_state_host(s2._h, hp)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        _lib.check(L.weno_solver_set_state_host(s2._h, hp, 8), "e2e set_state")
+        s2.run(1, graph=True)
+        _lib.check(L.weno_solver_get_state_host(s2._h, hp), "e2e get_state")
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": nx * ny * args.e2e_steps * world / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": M * N * 8 * 8, "d2h_bytes_per_step": M * N * 8 * 8,
+           "path": "weno_solver_set_state_host -> run(1) -> weno_solver_get_state_host, pinned host buffer"}
+    s2.close()
+
+    # ---- other variants (timed separately, graph replay) ----
+    variants = {}
+    if not args.no_variants:
+        for name, vkw, k in (("fp64_exact", dict(kw, mode="exact"), max(2, args.steps // 3)),
+                             ("fp32", dict(kw, precision=32, mode="fast"), args.steps * 4),
+                             ("fp64_fast_hllc_blend", dict(kw, force_hlle=False, jp_cri=(1e4, 1.1e4)),
+                              max(2, args.steps // 2))):
+            vms, vs = time_solver(weno_ext.Solver, q0, nx, ny, k, 3, **vkw)
+            variants[name] = {"value": nx * ny * k / (vms / 1e3), "unit": UNIT, "steps": k, "ms_per_step": vms / k}
+            vs.close()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"four-quadrant Riemann {nx}x{ny}, char-WENO5 + 2-pt Gauss faces + HLLE, "
+                               f"SSP-RK3, CFL 0.45, FP64 ({args.mode} arithmetic)",
+                   "nx": nx, "ny": ny, "seed": SEED, "mode": args.mode,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (state 4 x (nx+6)(ny+6) f64 = %.0f MB per buffer)" %
+                         (4 * M * N * 8 / 1e6)},
+        "roofline": roofline,
+        "compute_roofline": compute,
+        "kernels_ms": kern,
+        "clocks": clk,
+        "gpu_launches": launches,
+        "e2e": e2e,
+        "variants": variants,
+        "status": {"sim_time": t_sim, "steps_done": nsteps_done, "numeric_status": status},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(nx, int(os.environ.get("WENO_CPU_STRIP", "32")), os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line))
+    s.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

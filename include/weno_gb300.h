@@ -1,0 +1,153 @@
+/*
+ * weno_gb300.h -- C ABI of the GB300 (sm_103a) 2D Euler finite-volume step.
+ *
+ * The entry points replace the reference's PyO3 extension `weno_ext`
+ * (weno_ext/src/lib.rs, weno_ext/weno_ext.pyi).  Each function cites the
+ * reference interface it replaces.  All arrays are float64 unless stated;
+ * strides are in ELEMENTS and may be any (including negative) values.  Device
+ * entry points take device pointers and a cudaStream_t passed as void*; they
+ * only enqueue work (stream-ordered, asynchronous).  The caller owns every
+ * input, output and workspace buffer; the library allocates nothing on these
+ * paths (the *_host helpers and the solver own their device buffers).
+ *
+ * Arithmetic policy (`mode`):
+ *   WENO_EXACT  the reference's operation order with no FMA contraction: the
+ *               doubles are bit-identical to the Rust core's.
+ *   WENO_FAST   the same scheme with fewer FP64 divides and FMA contraction;
+ *               agrees with WENO_EXACT to rounding.
+ *
+ * Return value: WENO_OK (0) or an error code; weno_last_error() describes the
+ * last error of the calling thread.
+ */
+#ifndef WENO_GB300_H
+#define WENO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  WENO_OK = 0,
+  WENO_ERR_SHAPE = 1,     /* array too small / inconsistent shape (the reference panics) */
+  WENO_ERR_ARG = 2,       /* invalid argument value */
+  WENO_ERR_CUDA = 3,      /* a CUDA call failed */
+  WENO_ERR_WORKSPACE = 4, /* workspace missing or too small */
+  WENO_ERR_NUMERIC = 5    /* non-finite or non-positive wave speed met by the solver */
+};
+
+enum { WENO_EXACT = 0, WENO_FAST = 1 };
+
+/* Riemann solver selector of weno_riemann. */
+enum { WENO_HLLC = 0, WENO_HLLE = 1, WENO_BLEND = 2 };
+
+const char* weno_last_error(void);
+int weno_abi_version(void);
+
+/* Euler flux of channels 0..3 of q (m, n, c>=4), normal to x (ydir=0) or y.
+ * out: dense (m, n, 4).  Replaces flux_x_py / flux_y_py (lib.rs:18-30,
+ * utils.rs:74-109). */
+int weno_flux(const double* q, int64_t m, int64_t n, int64_t c, int64_t s0, int64_t s1, int64_t s2, double gamma,
+              int ydir, int mode, double* out, void* stream);
+
+/* Primitive variables of q (m, n, c>=4): six dense (m, n) planes p, a (sound
+ * speed), rho (clamped), u, v, h (total enthalpy).  Replaces con2primi_py
+ * (lib.rs:32-38, utils.rs:9-35). */
+int weno_con2primi(const double* q, int64_t m, int64_t n, int64_t c, int64_t s0, int64_t s1, int64_t s2,
+                   double gamma, int mode, double* p, double* a, double* rho, double* u, double* v, double* h,
+                   void* stream);
+
+/* WENO5 reconstruction with the 2-point Gauss-quadrature transverse pass.
+ * u: (m, n, c>=4), m, n >= 6.  Outputs q_l, f_l, q_r, f_r dense
+ * (m-5, n-6, 4) for ydir=0 and (m-6, n-5, 4) for ydir=1.  cons=0:
+ * characteristic projection (weno_x_py / weno_y_py, lib.rs:40-52,
+ * weno.rs:367-632); cons=1: component-wise (weno.rs:635-1071).
+ * Workspace: weno_reconstruct_workspace(m, n, ydir) bytes. */
+size_t weno_reconstruct_workspace(int64_t m, int64_t n, int ydir);
+int weno_reconstruct(const double* u, int64_t m, int64_t n, int64_t c, int64_t s0, int64_t s1, int64_t s2,
+                     double gamma, int ydir, int cons, int mode, double* q_l, double* f_l, double* q_r, double* f_r,
+                     void* ws, size_t ws_bytes, void* stream);
+
+/* Interface flux from dense (m, n, 4) face states and fluxes, in the order of
+ * lib.rs (q_l, f_l, q_r, f_r).  kind WENO_HLLC: hllc_x_rs_py / hllc_y_rs_py
+ * (lib.rs:54-74); WENO_HLLE: hlle_*_rs_py (lib.rs:76-96); WENO_BLEND: the
+ * pressure-gradient blend of hllc_hlle_*_rs_py with force_hlle=false
+ * (lib.rs:98-132, riemann.rs:352-486; requires m, n >= 2).  out: dense
+ * (m, n, 4).  Workspace: weno_riemann_workspace(m, n, kind) bytes (0 for
+ * HLLC/HLLE). */
+size_t weno_riemann_workspace(int64_t m, int64_t n, int kind);
+int weno_riemann(const double* q_l, const double* f_l, const double* q_r, const double* f_r, int64_t m, int64_t n,
+                 double gamma, int ydir, int kind, double jp_lo, double jp_hi, int mode, double* out, void* ws,
+                 size_t ws_bytes, void* stream);
+
+/* Residual L(U) = -(dF/dx + dG/dy) of u (m, n, c>=4) with 3 ghost cells on
+ * every side; out: dense (m-6, n-6, 4).  force_hlle selects HLLE, otherwise
+ * the HLLC/HLLE sensor blend with thresholds (jp_lo, jp_hi) (needs m, n >= 8).
+ * cons selects the component-wise reconstruction.  Replaces l_local_py
+ * (lib.rs:134-153, riemann.rs:489-541).  Workspace:
+ * weno_l_local_workspace(m, n, force_hlle) bytes. */
+size_t weno_l_local_workspace(int64_t m, int64_t n, int force_hlle);
+int weno_l_local(const double* u, int64_t m, int64_t n, int64_t c, int64_t s0, int64_t s1, int64_t s2, double dx,
+                 double gamma, int force_hlle, double jp_lo, double jp_hi, int cons, int mode, double* out, void* ws,
+                 size_t ws_bytes, void* stream);
+
+/* weno_l_local on HOST memory: copies u to the device, runs the residual and
+ * copies the (m-6, n-6, 4) result back; synchronous.  u must be C-contiguous
+ * (s0 = n*c, s1 = c, s2 = 1).  The library keeps one grow-only device buffer
+ * set per device for these calls and serialises them with a lock.  This is the
+ * call a Rust/C host of the reference would make in place of l_local_py. */
+int weno_l_local_host(const double* u, int64_t m, int64_t n, int64_t c, double dx, double gamma, int force_hlle,
+                      double jp_lo, double jp_hi, int cons, int mode, double* out);
+
+/* ------------------------------------------------------------------------
+ * Device-resident SSP-RK3 solver: the time loop of Rie_prob_2d_rs.py:169-207,
+ * 311-365 (bc_kind WENO_BC_TRANSMISSIVE) or double_mach_reflection.py:97-134,
+ * 229-260 (WENO_BC_DMR, unitest.py:207-227) with the state resident in HBM as
+ * four conserved planes of (nx+6) x (ny+6).  precision 64 or 32 (the FP32
+ * bulk variant computes dt in FP64).  The solver owns its device memory.
+ * ---------------------------------------------------------------------- */
+enum { WENO_BC_TRANSMISSIVE = 0, WENO_BC_DMR = 1 };
+
+typedef struct weno_solver weno_solver;
+
+int weno_solver_create(weno_solver** out, int64_t nx, int64_t ny, double dx, double gamma, int precision, int mode,
+                       int cons, int force_hlle, double jp_lo, double jp_hi, double cfl, int bc_kind, int64_t bound,
+                       const double* post8, void* stream);
+int weno_solver_destroy(weno_solver* s);
+/* Load the state from a device array (nx+6, ny+6, c>=4).  With c >= 8 the
+ * first step's dt uses the primitive channels 5..7 as the driver does. */
+int weno_solver_set_state(weno_solver* s, const double* q, int64_t c, int64_t s0, int64_t s1, int64_t s2);
+int weno_solver_set_state_host(weno_solver* s, const double* q, int64_t c);
+/* Enqueue nsteps steps.  t_final < 0: step-count mode; otherwise steps stop
+ * (as device-side no-ops) once t >= t_final - 1e-12, dt clipped to the time
+ * left.  use_graph=1 replays a captured CUDA graph of one step. */
+int weno_solver_run(weno_solver* s, int64_t nsteps, double t_final, int use_graph);
+/* The driver's (nx+6, ny+6, 8) array: conserved channels and the primitive
+ * sync (rho_safe, u, v, p), then the boundary fill on all eight channels. */
+int weno_solver_get_state(weno_solver* s, double* out);
+int weno_solver_get_state_host(weno_solver* s, double* out);
+/* Synchronise and read the clock: simulated time, completed steps, status
+ * (0 ok, else WENO_ERR_NUMERIC). */
+int weno_solver_info(weno_solver* s, double* t, int64_t* steps, int* status);
+/* CUDA-event timing of kernel groups, recorded on the solver's stream during
+ * runs with use_graph=0.  Classes: 0 CFL reduction + dt, 1 boundary fills,
+ * 2 x pass 1, 3 x pass 2, 4 sensor blends, 5 y pass 1, 6 y pass 2,
+ * 7 residual + stage combination.  Enabling resets the record; the report
+ * synchronises and returns the summed milliseconds and launch-group counts. */
+int weno_solver_enable_timing(weno_solver* s, int on);
+int weno_solver_timing_report(weno_solver* s, double* ms, int64_t* launches, int nclasses);
+/* Number of kernel launches one step enqueues (for launch accounting). */
+int weno_solver_launches_per_step(weno_solver* s);
+
+/* Diagnostics: measured FP64 FMA (TFLOP/s), FP64 divide (per s) and FP32 FMA
+ * (TFLOP/s) throughput of the current device -- the compute-roofline
+ * denominators, with no counterpart in the reference. */
+int weno_probe_rates(double* fp64_tflops, double* fp64_div_per_s, double* fp32_tflops, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WENO_GB300_H */

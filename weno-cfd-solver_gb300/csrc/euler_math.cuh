@@ -1,0 +1,591 @@
+// Device arithmetic of the 2D Euler finite-volume residual.
+//
+// Every function follows the reference's Rust core (weno_ext/src/utils.rs,
+// weno.rs, riemann.rs) and is templated on
+//   T    -- double or float, the arithmetic type;
+//   FAST -- false: the reference's operation order, so that a translation unit
+//           compiled with --fmad=false reproduces the Rust IEEE-754 doubles bit
+//           for bit; true: the same mathematics with fewer FP64 divisions
+//           (shared reciprocals, a common-denominator form of the WENO weights)
+//           and FMA contraction, checked against the oracle by tolerance.
+//
+// GB300 executes FP64 at 1/64 of the FP32 rate and a correctly rounded FP64
+// divide costs about ten FMA slots, so the FAST forms are written to remove
+// divides and square roots rather than memory traffic.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#ifndef WENO_TU_NS
+#error "WENO_TU_NS names the translation unit's inline namespace (tu_exact or tu_fast)"
+#endif
+
+namespace weno {
+// Each translation unit compiles its kernels into its own inline namespace, so
+// the --fmad=false and --fmad=true builds of the same template never share a
+// symbol (the linker would otherwise keep only one of them).
+inline namespace WENO_TU_NS {
+
+// utils.rs:3-6
+constexpr double kEps = 1e-12;              // DEFAULT_EPS, RHO_MIN and P_MIN
+constexpr double kSqrt3_12 = 0.1443375673;  // truncated literal, not sqrt(3)/12
+// weno.rs:270 / weno.rs:292 (Gauss-point linear weights, 10 digits)
+constexpr double kGqA0 = 0.1928406937, kGqA1 = 0.6111111111, kGqA2 = 0.1960481952;
+constexpr double kC13 = 13.0 / 12.0;
+
+template <class T>
+__device__ __forceinline__ T vmax(T a, T b) { return fmax(a, b); }
+template <class T>
+__device__ __forceinline__ T vmin(T a, T b) { return fmin(a, b); }
+
+// a / b: the IEEE quotient except in FAST float, which uses the SFU path.
+template <class T, bool FAST>
+__device__ __forceinline__ T qdiv(T a, T b) {
+  if constexpr (FAST && sizeof(T) == 4) return __fdividef(a, b);
+  else return a / b;
+}
+template <class T, bool FAST>
+__device__ __forceinline__ T qrcp(T b) {
+  if constexpr (FAST && sizeof(T) == 4) return __fdividef(1.0f, b);
+  else return T(1.0) / b;
+}
+
+// ---------------------------------------------------------------------------
+// Conserved state helpers (utils.rs:9-35, utils.rs:74-109)
+// ---------------------------------------------------------------------------
+// Euler flux normal to x (Y = false) or y (Y = true), utils.rs:74-109.
+template <class T, bool FAST, bool Y>
+__device__ __forceinline__ void euler_flux(const T q[4], T gamma, T f[4]) {
+  const T rho = vmax(q[0], T(kEps));
+  T u, v;
+  if constexpr (FAST) {
+    const T r = qrcp<T, FAST>(rho);
+    u = q[1] * r;
+    v = q[2] * r;
+  } else {
+    u = q[1] / rho;
+    v = q[2] / rho;
+  }
+  const T p = (gamma - T(1.0)) * (q[3] - T(0.5) * rho * (u * u + v * v));
+  if constexpr (!Y) {
+    f[0] = q[1];
+    f[1] = q[1] * u + p;
+    f[2] = q[2] * u;
+    f[3] = u * (q[3] + p);
+  } else {
+    f[0] = q[2];
+    f[1] = q[1] * v;
+    f[2] = q[2] * v + p;
+    f[3] = v * (q[3] + p);
+  }
+}
+
+// utils.rs:9-35 con2primi_local for one cell.
+template <class T, bool FAST>
+__device__ __forceinline__ void con2prim(T q0, T q1, T q2, T q3, T gamma, T& p, T& a, T& rho, T& u, T& v, T& h) {
+  rho = vmax(q0, T(kEps));
+  if constexpr (FAST) {
+    const T r = qrcp<T, FAST>(rho);
+    u = q1 * r;
+    v = q2 * r;
+    p = vmax((gamma - T(1.0)) * (q3 - T(0.5) * rho * (u * u + v * v)), T(kEps));
+    a = sqrt(gamma * p * r);
+    h = (q3 + p) * r;
+  } else {
+    u = q1 / rho;
+    v = q2 / rho;
+    p = vmax((gamma - T(1.0)) * (q3 - T(0.5) * rho * (u * u + v * v)), T(kEps));
+    a = sqrt(gamma * p / rho);
+    h = (q3 + p) / rho;
+  }
+}
+
+// Pressure of con2primi (clamped density and pressure) -- the quantity the
+// shock sensor averages (riemann.rs:421-430).
+template <class T, bool FAST>
+__device__ __forceinline__ T clamped_pressure(const T q[4], T gamma) {
+  const T rho = vmax(q[0], T(kEps));
+  T u, v;
+  if constexpr (FAST) {
+    const T r = qrcp<T, FAST>(rho);
+    u = q[1] * r;
+    v = q[2] * r;
+  } else {
+    u = q[1] / rho;
+    v = q[2] / rho;
+  }
+  return vmax((gamma - T(1.0)) * (q[3] - T(0.5) * rho * (u * u + v * v)), T(kEps));
+}
+
+// ---------------------------------------------------------------------------
+// WENO5-JS (weno.rs:214-257) and the 2-point Gauss-quadrature pair
+// (weno.rs:262-303).
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ void js_betas(T u0, T u1, T u2, T u3, T u4, T& b0, T& b1, T& b2) {
+  T t, s;
+  t = u2 - T(2.0) * u3 + u4;
+  s = T(3.0) * u2 - T(4.0) * u3 + u4;
+  b0 = T(kC13) * (t * t) + T(0.25) * (s * s);
+  t = u1 - T(2.0) * u2 + u3;
+  s = u1 - u3;
+  b1 = T(kC13) * (t * t) + T(0.25) * (s * s);
+  t = u0 - T(2.0) * u1 + u2;
+  s = u0 - T(4.0) * u1 + T(3.0) * u2;
+  b2 = T(kC13) * (t * t) + T(0.25) * (s * s);
+}
+
+// Power-of-two scale that brings x (> 0, finite) into [0.5, 1): multiplying
+// by it is exact, and its exponent comes from integer operations, so no FP64
+// pipe slot is spent.  Returns 1 for zero, denormal or non-finite x.
+__device__ __forceinline__ double pow2_scale_of(double x) {
+  const int hi = __double2hiint(x);
+  const int e = (hi >> 20) & 0x7ff;  // biased exponent
+  if (e == 0 || e == 0x7ff) return 1.0;
+  // 2^(1022 - e) has biased exponent 2045 - e; clamp to the normal range
+  // (x >= 2^1022 then lands in [0.5, 4), still safe for the products).
+  int b = 2045 - e;
+  if (b < 1) b = 1;
+  return __hiloint2double(b << 20, 0);
+}
+
+// Non-linear weighting of three candidate values with linear weights d.
+// Exact: the reference's a_k = d_k/(eps+b_k)^2, w_k = a_k/sum.
+// FAST double: one divide via the common denominator prod_j (eps+b_j)^2,
+// with the three (eps+b_k) first scaled by the same power of two so that the
+// largest lies in [0.5, 1) -- the products then neither overflow nor lose the
+// dominant weight, whatever the magnitude of the stencil values.
+// FAST float: reciprocals, because FP32 would underflow the products.
+template <class T, bool FAST>
+__device__ __forceinline__ T weno_combine(T e0, T e1, T e2, T d0, T d1, T d2, T p0, T p1, T p2, T scale) {
+  if constexpr (!FAST) {
+    const T a0 = d0 / (e0 * e0);
+    const T a1 = d1 / (e1 * e1);
+    const T a2 = d2 / (e2 * e2);
+    const T sum = a0 + a1 + a2;
+    const T w0 = a0 / sum, w1 = a1 / sum, w2 = a2 / sum;
+    const T r = w0 * p0 + w1 * p1 + w2 * p2;
+    return scale == T(1.0) ? r : r / scale;
+  } else if constexpr (sizeof(T) == 8) {
+    const T sc = pow2_scale_of(fmax(fmax(e0, e1), e2));
+    e0 *= sc;
+    e1 *= sc;
+    e2 *= sc;
+    const T s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
+    const T c0 = d0 * (s1 * s2), c1 = d1 * (s0 * s2), c2 = d2 * (s0 * s1);
+    const T num = c0 * p0 + c1 * p1 + c2 * p2;
+    const T den = (c0 + c1 + c2) * scale;
+    return num / den;
+  } else {
+    const T a0 = d0 * qrcp<T, FAST>(e0 * e0);
+    const T a1 = d1 * qrcp<T, FAST>(e1 * e1);
+    const T a2 = d2 * qrcp<T, FAST>(e2 * e2);
+    const T num = a0 * p0 + a1 * p1 + a2 * p2;
+    return qdiv<T, FAST>(num, (a0 + a1 + a2) * scale);
+  }
+}
+
+// weno.rs:214-233 (left-biased, value at the right face of u2)
+template <class T, bool FAST>
+__device__ __forceinline__ T weno5_left(T u0, T u1, T u2, T u3, T u4) {
+  T b0, b1, b2;
+  js_betas(u0, u1, u2, u3, u4, b0, b1, b2);
+  const T p0 = -u4 + T(5.0) * u3 + T(2.0) * u2;
+  const T p1 = -u1 + T(5.0) * u2 + T(2.0) * u3;
+  const T p2 = T(2.0) * u0 - T(7.0) * u1 + T(11.0) * u2;
+  return weno_combine<T, FAST>(T(kEps) + b0, T(kEps) + b1, T(kEps) + b2, T(0.3), T(0.6), T(0.1), p0, p1, p2, T(6.0));
+}
+
+// weno.rs:238-257 (right-biased, value at the left face of u3)
+template <class T, bool FAST>
+__device__ __forceinline__ T weno5_right(T u1, T u2, T u3, T u4, T u5) {
+  T b0, b1, b2;
+  T t, s;
+  t = u3 - T(2.0) * u4 + u5;
+  s = T(3.0) * u3 - T(4.0) * u4 + u5;
+  b0 = T(kC13) * (t * t) + T(0.25) * (s * s);
+  t = u2 - T(2.0) * u3 + u4;
+  s = u2 - u4;
+  b1 = T(kC13) * (t * t) + T(0.25) * (s * s);
+  t = u1 - T(2.0) * u2 + u3;
+  s = u1 - T(4.0) * u2 + T(3.0) * u3;
+  b2 = T(kC13) * (t * t) + T(0.25) * (s * s);
+  const T p0 = T(2.0) * u5 - T(7.0) * u4 + T(11.0) * u3;
+  const T p1 = -u4 + T(5.0) * u3 + T(2.0) * u2;
+  const T p2 = -u1 + T(5.0) * u2 + T(2.0) * u3;
+  return weno_combine<T, FAST>(T(kEps) + b0, T(kEps) + b1, T(kEps) + b2, T(0.1), T(0.6), T(0.3), p0, p1, p2, T(6.0));
+}
+
+// weno.rs:262-303: both Gauss-point values from one 5-cell stencil.  The
+// smoothness indicators are shared (the reference recomputes identical values).
+template <class T, bool FAST>
+__device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& ra, T& rb) {
+  T b0, b1, b2;
+  js_betas(q0, q1, q2, q3, q4, b0, b1, b2);
+  const T e0 = T(kEps) + b0, e1 = T(kEps) + b1, e2 = T(kEps) + b2;
+  const T S = T(kSqrt3_12);
+  const T g0 = T(3.0) * q2 - T(4.0) * q3 + q4;
+  const T g2 = T(3.0) * q2 - T(4.0) * q1 + q0;
+  if constexpr (!FAST) {
+    const T pa0 = q2 + g0 * S;
+    const T pa1 = q2 - (-q1 + q3) * S;
+    const T pa2 = q2 - g2 * S;
+    ra = weno_combine<T, FAST>(e0, e1, e2, T(kGqA0), T(kGqA1), T(kGqA2), pa0, pa1, pa2, T(1.0));
+    const T pb0 = q2 - g0 * S;
+    const T pb1 = q2 - (q1 - q3) * S;
+    const T pb2 = q2 + g2 * S;
+    rb = weno_combine<T, FAST>(e0, e1, e2, T(kGqA2), T(kGqA1), T(kGqA0), pb0, pb1, pb2, T(1.0));
+  } else {
+    const T g1 = (q3 - q1) * S;
+    const T pa0 = q2 + g0 * S, pa1 = q2 - g1, pa2 = q2 - g2 * S;
+    const T pb0 = q2 - g0 * S, pb1 = q2 + g1, pb2 = q2 + g2 * S;
+    if constexpr (sizeof(T) == 8) {
+      const T sc = pow2_scale_of(fmax(fmax(e0, e1), e2));
+      const T f0 = e0 * sc, f1 = e1 * sc, f2 = e2 * sc;
+      const T s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
+      const T P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
+      const T ca0 = T(kGqA0) * P0, ca1 = T(kGqA1) * P1, ca2 = T(kGqA2) * P2;
+      const T cb0 = T(kGqA2) * P0, cb2 = T(kGqA0) * P2;
+      const T inv = T(1.0) / ((ca0 + ca1 + ca2) * (cb0 + ca1 + cb2));
+      ra = (ca0 * pa0 + ca1 * pa1 + ca2 * pa2) * (cb0 + ca1 + cb2) * inv;
+      rb = (cb0 * pb0 + ca1 * pb1 + cb2 * pb2) * (ca0 + ca1 + ca2) * inv;
+    } else {
+      const T r0 = qrcp<T, FAST>(e0 * e0), r1 = qrcp<T, FAST>(e1 * e1), r2 = qrcp<T, FAST>(e2 * e2);
+      const T ca0 = T(kGqA0) * r0, ca1 = T(kGqA1) * r1, ca2 = T(kGqA2) * r2;
+      const T cb0 = T(kGqA2) * r0, cb2 = T(kGqA0) * r2;
+      ra = qdiv<T, FAST>(ca0 * pa0 + ca1 * pa1 + ca2 * pa2, ca0 + ca1 + ca2);
+      rb = qdiv<T, FAST>(cb0 * pb0 + ca1 * pb1 + cb2 * pb2, cb0 + ca1 + cb2);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Characteristic projection (weno.rs:13-205)
+// ---------------------------------------------------------------------------
+// Roe average of two conserved cells, weno.rs:13-52.
+template <class T, bool FAST>
+__device__ __forceinline__ void roe_avg(const T ul[4], const T ur[4], T gamma, T& rho_roe, T& u_roe, T& v_roe,
+                                        T& h_roe, T& c_roe) {
+  const T rho_l = vmax(ul[0], T(kEps));
+  const T rho_r = vmax(ur[0], T(kEps));
+  const T sqrt_l = sqrt(rho_l);
+  const T sqrt_r = sqrt(rho_r);
+  const T denom = sqrt_l + sqrt_r;
+  if constexpr (!FAST) {
+    const T u_l = ul[1] / rho_l, v_l = ul[2] / rho_l;
+    const T u_r = ur[1] / rho_r, v_r = ur[2] / rho_r;
+    const T p_l = vmax((gamma - T(1.0)) * (ul[3] - T(0.5) * rho_l * (u_l * u_l + v_l * v_l)), T(kEps));
+    const T p_r = vmax((gamma - T(1.0)) * (ur[3] - T(0.5) * rho_r * (u_r * u_r + v_r * v_r)), T(kEps));
+    const T h_l = (ul[3] + p_l) / rho_l;
+    const T h_r = (ur[3] + p_r) / rho_r;
+    u_roe = (sqrt_l * u_l + sqrt_r * u_r) / denom;
+    v_roe = (sqrt_l * v_l + sqrt_r * v_r) / denom;
+    h_roe = (sqrt_l * h_l + sqrt_r * h_r) / denom;
+  } else {
+    const T il = qrcp<T, FAST>(rho_l), ir = qrcp<T, FAST>(rho_r);
+    const T u_l = ul[1] * il, v_l = ul[2] * il;
+    const T u_r = ur[1] * ir, v_r = ur[2] * ir;
+    const T p_l = vmax((gamma - T(1.0)) * (ul[3] - T(0.5) * rho_l * (u_l * u_l + v_l * v_l)), T(kEps));
+    const T p_r = vmax((gamma - T(1.0)) * (ur[3] - T(0.5) * rho_r * (u_r * u_r + v_r * v_r)), T(kEps));
+    const T h_l = (ul[3] + p_l) * il;
+    const T h_r = (ur[3] + p_r) * ir;
+    const T id = qrcp<T, FAST>(denom);
+    u_roe = (sqrt_l * u_l + sqrt_r * u_r) * id;
+    v_roe = (sqrt_l * v_l + sqrt_r * v_r) * id;
+    h_roe = (sqrt_l * h_l + sqrt_r * h_r) * id;
+  }
+  const T kin = T(0.5) * (u_roe * u_roe + v_roe * v_roe);
+  T c2;
+  if constexpr (!FAST) c2 = vmax((gamma - T(1.0)) * (h_roe - kin), T(kEps) / vmin(rho_l, rho_r));
+  else c2 = vmax((gamma - T(1.0)) * (h_roe - kin), T(kEps) * vmax(qrcp<T, FAST>(rho_l), qrcp<T, FAST>(rho_r)));
+  c_roe = sqrt(c2);
+  rho_roe = sqrt_l * sqrt_r;
+}
+
+// Left eigenvectors, weno.rs:76-107 (x) and weno.rs:136-167 (y).
+template <class T, bool FAST, bool Y>
+__device__ __forceinline__ void left_eig(T rho, T u, T v, T c, T gamma, T L[4][4]) {
+  const T g1 = gamma - T(1.0);
+  const T kin = T(0.5) * (u * u + v * v);
+  T inv_rc, inv_c2, a, b, irho;
+  const T vn = Y ? v : u;
+  if constexpr (!FAST) {
+    const T rc = rho * c;
+    inv_rc = T(1.0) / rc;
+    inv_c2 = T(1.0) / (c * c);
+    a = g1 * kin / (T(2.0) * c * c);
+    b = vn / (T(2.0) * c);
+  } else {
+    const T ic = qrcp<T, FAST>(c);
+    irho = qrcp<T, FAST>(rho);
+    inv_rc = ic * irho;
+    inv_c2 = ic * ic;
+    a = T(0.5) * (g1 * kin) * inv_c2;
+    b = T(0.5) * vn * ic;
+  }
+  const T gu = -g1 * u * inv_c2 / T(2.0);
+  const T gv = -g1 * v * inv_c2 / T(2.0);
+  const T gg = g1 * inv_c2 / T(2.0);
+  const T hr = T(0.5) * inv_rc;
+  L[0][0] = a + b;
+  L[3][0] = a - b;
+  if constexpr (!Y) {
+    L[0][1] = gu - hr; L[0][2] = gv; L[0][3] = gg;
+    L[3][1] = gu + hr; L[3][2] = gv; L[3][3] = gg;
+    if constexpr (!FAST) {
+      L[2][0] = -v / rho; L[2][1] = T(0.0); L[2][2] = T(1.0) / rho; L[2][3] = T(0.0);
+    } else {
+      L[2][0] = -v * irho; L[2][1] = T(0.0); L[2][2] = irho; L[2][3] = T(0.0);
+    }
+  } else {
+    L[0][1] = gu; L[0][2] = gv - hr; L[0][3] = gg;
+    L[3][1] = gu; L[3][2] = gv + hr; L[3][3] = gg;
+    if constexpr (!FAST) {
+      L[2][0] = -u / rho; L[2][1] = T(1.0) / rho; L[2][2] = T(0.0); L[2][3] = T(0.0);
+    } else {
+      L[2][0] = -u * irho; L[2][1] = irho; L[2][2] = T(0.0); L[2][3] = T(0.0);
+    }
+  }
+  L[1][0] = T(1.0) - g1 * kin * inv_c2;
+  L[1][1] = g1 * u * inv_c2;
+  L[1][2] = g1 * v * inv_c2;
+  L[1][3] = -g1 * inv_c2;
+}
+
+// Right eigenvectors, weno.rs:113-131 (x) and weno.rs:171-189 (y).
+template <class T, bool Y>
+__device__ __forceinline__ void right_eig(T rho, T u, T v, T h, T c, T R[4][4]) {
+  const T kin = T(0.5) * (u * u + v * v);
+  R[0][0] = T(1.0); R[0][1] = T(1.0); R[0][2] = T(0.0); R[0][3] = T(1.0);
+  if constexpr (!Y) {
+    R[1][0] = u - c; R[1][1] = u; R[1][2] = T(0.0); R[1][3] = u + c;
+    R[2][0] = v; R[2][1] = v; R[2][2] = rho; R[2][3] = v;
+    R[3][0] = h - u * c; R[3][1] = kin; R[3][2] = rho * v; R[3][3] = h + u * c;
+  } else {
+    R[1][0] = u; R[1][1] = u; R[1][2] = rho; R[1][3] = u;
+    R[2][0] = v - c; R[2][1] = v; R[2][2] = T(0.0); R[2][3] = v + c;
+    R[3][0] = h - v * c; R[3][1] = kin; R[3][2] = rho * u; R[3][3] = h + v * c;
+  }
+}
+
+// weno.rs:197-205 mat4_vec4: exact mode accumulates every product from 0.0 in
+// column order; FAST skips the structural zeros of the eigenvector matrices.
+template <class T, bool FAST>
+__device__ __forceinline__ void mat4_vec4(const T M[4][4], const T x[4], T out[4]) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    if constexpr (!FAST) {
+      T acc = T(0.0);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc = acc + M[r][c] * x[c];
+      out[r] = acc;
+    } else {
+      out[r] = M[r][0] * x[0] + M[r][1] * x[1] + M[r][2] * x[2] + M[r][3] * x[3];
+    }
+  }
+}
+
+// weno.rs:312-315 pressure ; weno.rs:327-352 Zhang-Shu limiter toward `ub`.
+template <class T, bool FAST>
+__device__ __forceinline__ T pp_pressure(const T q[4], T gamma) {
+  if (q[0] <= T(0.0)) return T(0.0);
+  return (gamma - T(1.0)) * (q[3] - qdiv<T, FAST>(T(0.5) * (q[1] * q[1] + q[2] * q[2]), q[0]));
+}
+template <class T, bool FAST>
+__device__ __forceinline__ void pp_limit(T q[4], const T ub[4], T gamma) {
+  if (q[0] < T(kEps)) {
+    const T rho_bar = vmax(ub[0], T(kEps));
+    const T theta = vmax(vmin(qdiv<T, FAST>(rho_bar - T(kEps), rho_bar - q[0]), T(1.0)), T(0.0));
+#pragma unroll
+    for (int k = 0; k < 4; ++k) q[k] = theta * (q[k] - ub[k]) + ub[k];
+  }
+  const T p_q = pp_pressure<T, FAST>(q, gamma);
+  if (p_q < T(kEps)) {
+    const T p_bar = vmax(pp_pressure<T, FAST>(ub, gamma), T(kEps));
+    const T theta = vmax(vmin(qdiv<T, FAST>(p_bar - T(kEps), p_bar - p_q), T(1.0)), T(0.0));
+#pragma unroll
+    for (int k = 0; k < 4; ++k) q[k] = theta * (q[k] - ub[k]) + ub[k];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pass 1: normal-direction reconstruction of the two states at the interface
+// between stencil cells 2 and 3 (weno.rs:390-454 characteristic,
+// weno.rs:654-717 component-wise).  c[0..5] are the six cells along the normal.
+// ---------------------------------------------------------------------------
+template <class T, bool FAST, bool Y, bool CHAR>
+__device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T qr[4]) {
+  if constexpr (!CHAR) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      ql[k] = weno5_left<T, FAST>(c[0][k], c[1][k], c[2][k], c[3][k], c[4][k]);
+      qr[k] = weno5_right<T, FAST>(c[1][k], c[2][k], c[3][k], c[4][k], c[5][k]);
+    }
+  } else {
+    T rho_a, u_a, v_a, h_a, c_a;
+    roe_avg<T, FAST>(c[2], c[3], gamma, rho_a, u_a, v_a, h_a, c_a);
+    T Lm[4][4];
+    left_eig<T, FAST, Y>(rho_a, u_a, v_a, c_a, gamma, Lm);
+    // The reference projects cells 0..4 for the left state and 1..5 for the
+    // right state with the same matrix (both faces use the Roe average of
+    // cells 2|3), so six projections cover both.
+    T w[6][4];
+#pragma unroll
+    for (int s = 0; s < 6; ++s) mat4_vec4<T, FAST>(Lm, c[s], w[s]);
+    T chl[4], chr[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      chl[k] = weno5_left<T, FAST>(w[0][k], w[1][k], w[2][k], w[3][k], w[4][k]);
+      chr[k] = weno5_right<T, FAST>(w[1][k], w[2][k], w[3][k], w[4][k], w[5][k]);
+    }
+    T Rm[4][4];
+    right_eig<T, Y>(rho_a, u_a, v_a, h_a, c_a, Rm);
+    mat4_vec4<T, FAST>(Rm, chl, ql);
+    mat4_vec4<T, FAST>(Rm, chr, qr);
+    pp_limit<T, FAST>(ql, c[2], gamma);
+    pp_limit<T, FAST>(qr, c[3], gamma);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Interface Riemann solvers (riemann.rs:6-349).  Inputs are the face-averaged
+// states and fluxes; `ql`/`qr` are the raw (unclamped) states.
+// ---------------------------------------------------------------------------
+template <class T, bool FAST, bool Y>
+struct RiemannPre {
+  T ql0, qr0, u_l, v_l, u_r, v_r, p_l, p_r, s_l, s_r, un_l, un_r;
+};
+
+template <class T, bool FAST, bool Y>
+__device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], const T qr[4], T gamma) {
+  RiemannPre<T, FAST, Y> r;
+  r.ql0 = vmax(ql[0], T(kEps));
+  r.qr0 = vmax(qr[0], T(kEps));
+  T h_l, h_r, u_t, v_t, h_t;
+  if constexpr (!FAST) {
+    r.u_l = ql[1] / r.ql0; r.v_l = ql[2] / r.ql0;
+    r.u_r = qr[1] / r.qr0; r.v_r = qr[2] / r.qr0;
+  } else {
+    const T il = qrcp<T, FAST>(r.ql0), ir = qrcp<T, FAST>(r.qr0);
+    r.u_l = ql[1] * il; r.v_l = ql[2] * il;
+    r.u_r = qr[1] * ir; r.v_r = qr[2] * ir;
+  }
+  // FAST: sqrt(rho)*u = q1/sqrt(rho) and sqrt(rho)*h = (E+p)/sqrt(rho).
+  r.p_l = (gamma - T(1.0)) * (ql[3] - T(0.5) * r.ql0 * (r.u_l * r.u_l + r.v_l * r.v_l));
+  r.p_r = (gamma - T(1.0)) * (qr[3] - T(0.5) * r.qr0 * (r.u_r * r.u_r + r.v_r * r.v_r));
+  r.p_l = vmax(r.p_l, T(kEps));
+  r.p_r = vmax(r.p_r, T(kEps));
+  const T srl = sqrt(r.ql0), srr = sqrt(r.qr0);
+  const T denom_r = srl + srr;
+  if constexpr (!FAST) {
+    h_l = (ql[3] + r.p_l) / r.ql0;
+    h_r = (qr[3] + r.p_r) / r.qr0;
+    u_t = (srl * r.u_l + srr * r.u_r) / denom_r;
+    v_t = (srl * r.v_l + srr * r.v_r) / denom_r;
+    h_t = (srl * h_l + srr * h_r) / denom_r;
+  } else {
+    // sqrt(rho)*h = (E+p)/sqrt(rho): one reciprocal square root per side.
+    const T il = qrcp<T, FAST>(srl), ir = qrcp<T, FAST>(srr);
+    const T id = qrcp<T, FAST>(denom_r);
+    u_t = (ql[1] * il + qr[1] * ir) * id;
+    v_t = (ql[2] * il + qr[2] * ir) * id;
+    h_t = ((ql[3] + r.p_l) * il + (qr[3] + r.p_r) * ir) * id;
+  }
+  const T tmp = h_t - T(0.5) * (u_t * u_t + v_t * v_t);
+  const T a_t = sqrt(vmax((gamma - T(1.0)) * tmp, T(0.0)));
+  const T un_t = Y ? v_t : u_t;
+  r.un_l = Y ? r.v_l : r.u_l;
+  r.un_r = Y ? r.v_r : r.u_r;
+  r.s_l = un_t - a_t;
+  r.s_r = un_t + a_t;
+  return r;
+}
+
+template <class T>
+__device__ __forceinline__ T guard_denom(T d) {
+  if (fabs(d) < T(kEps)) d = copysign(T(kEps), d) + T(kEps);
+  return d;
+}
+
+// riemann.rs:191-349 HLLE
+template <class T, bool FAST, bool Y>
+__device__ __forceinline__ void hlle_flux(const RiemannPre<T, FAST, Y>& r, const T ql[4], const T fl[4],
+                                          const T qr[4], const T fr[4], T F[4]) {
+  const T denom = guard_denom(r.s_r - r.s_l);
+  if (r.s_l >= T(0.0)) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) F[k] = fl[k];
+  } else if (r.s_r < T(0.0)) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) F[k] = fr[k];
+  } else {
+    const T qlv[4] = {r.ql0, ql[1], ql[2], ql[3]};
+    const T qrv[4] = {r.qr0, qr[1], qr[2], qr[3]};
+    const T srsl = r.s_r * r.s_l;
+    if constexpr (!FAST) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) F[k] = (r.s_r * fl[k] - r.s_l * fr[k] + srsl * (qrv[k] - qlv[k])) / denom;
+    } else {
+      const T id = qrcp<T, FAST>(denom);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) F[k] = (r.s_r * fl[k] - r.s_l * fr[k] + srsl * (qrv[k] - qlv[k])) * id;
+    }
+  }
+}
+
+// riemann.rs:6-189 HLLC
+template <class T, bool FAST, bool Y>
+__device__ __forceinline__ void hllc_flux(const RiemannPre<T, FAST, Y>& r, const T ql[4], const T fl[4],
+                                          const T qr[4], const T fr[4], T F[4]) {
+  if (r.s_l >= T(0.0)) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) F[k] = fl[k];
+    return;
+  }
+  const T denom = guard_denom(r.ql0 * (r.s_l - r.un_l) - r.qr0 * (r.s_r - r.un_r));
+  const T s_star = qdiv<T, FAST>(
+      r.p_r - r.p_l + r.ql0 * r.un_l * (r.s_l - r.un_l) - r.qr0 * r.un_r * (r.s_r - r.un_r), denom);
+  if (r.s_l < T(0.0) && s_star >= T(0.0)) {
+    // left star state
+    const T m_l = r.ql0 * (r.s_l - r.un_l);
+    const T coeff = qdiv<T, FAST>(m_l, r.s_l - s_star);
+    const T e_spec = qdiv<T, FAST>(ql[3], r.ql0);
+    const T e_star = e_spec + (s_star - r.un_l) * (s_star + qdiv<T, FAST>(r.p_l, m_l));
+    T qs[4];
+    qs[0] = coeff;
+    qs[1] = Y ? coeff * r.u_l : coeff * s_star;
+    qs[2] = Y ? coeff * s_star : coeff * r.v_l;
+    qs[3] = coeff * e_star;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) F[k] = fl[k] + r.s_l * (qs[k] - ql[k]);
+  } else if (s_star < T(0.0) && r.s_r > T(0.0)) {
+    const T m_r = r.qr0 * (r.s_r - r.un_r);
+    const T coeff = qdiv<T, FAST>(m_r, r.s_r - s_star);
+    const T e_spec = qdiv<T, FAST>(qr[3], r.qr0);
+    const T e_star = e_spec + (s_star - r.un_r) * (s_star + qdiv<T, FAST>(r.p_r, m_r));
+    T qs[4];
+    qs[0] = coeff;
+    qs[1] = Y ? coeff * r.u_r : coeff * s_star;
+    qs[2] = Y ? coeff * s_star : coeff * r.v_r;
+    qs[3] = coeff * e_star;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) F[k] = fr[k] + r.s_r * (qs[k] - qr[k]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) F[k] = fr[k];
+  }
+}
+
+// riemann.rs:394-405: blend weight from the normalised pressure gradient.
+template <class T, bool FAST>
+__device__ __forceinline__ T sensor_weight(T dpdx, T dpdy, T p, T jp_lo, T jp_hi) {
+  const T grad = sqrt(dpdx * dpdx + dpdy * dpdy);
+  const T jp = qdiv<T, FAST>(grad, vmax(p, T(kEps)));
+  if (jp <= jp_lo) return T(1.0);
+  if (jp >= jp_hi) return T(0.0);
+  return T(1.0) - qdiv<T, FAST>(jp - jp_lo, jp_hi - jp_lo);
+}
+
+}  // inline namespace WENO_TU_NS
+}  // namespace weno
