@@ -93,6 +93,22 @@ int weno_l_local(const double* u, int64_t m, int64_t n, int64_t c, int64_t s0, i
                  double gamma, int force_hlle, double jp_lo, double jp_hi, int cons, int mode, double* out, void* ws,
                  size_t ws_bytes, void* stream);
 
+/* weno_l_local without a caller workspace and without any allocation: the
+ * scratch is a 64 MiB array owned by the library (a static device array that
+ * every GPU loading the library holds until exit).  No counterpart in the
+ * reference.  For callers that cannot allocate device memory -- a host that
+ * owns all device memory through its own pool, a loop that must not pay
+ * cudaMalloc's device-wide synchronisation, code recorded into a CUDA graph.
+ * Limit: weno_l_local_workspace(m, n, force_hlle) <= 64 MiB, i.e. about
+ * 720 x 720 cells with HLLE and 560 x 560 with the blend (FP64); larger arrays
+ * return WENO_ERR_WORKSPACE.  All calls on a device share the array: calls
+ * that overlap on the GPU race and must be ordered by the caller.  The first
+ * call on a device looks up the array's address (may load the module): make
+ * it before any stream capture. */
+int weno_l_local_noalloc(const double* u, int64_t m, int64_t n, int64_t c, int64_t s0, int64_t s1, int64_t s2,
+                         double dx, double gamma, int force_hlle, double jp_lo, double jp_hi, int cons, int mode,
+                         double* out, void* stream);
+
 /* weno_l_local on HOST memory: copies u to the device, runs the residual and
  * copies the (m-6, n-6, 4) result back; synchronous.  u must be C-contiguous
  * (s0 = n*c, s1 = c, s2 = 1).  The library keeps one grow-only device buffer

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/weno_gb300.h"
+#include "errors.h"
 #include "launch_api.h"
 #include "step_ctl.h"
 
@@ -141,6 +142,13 @@ int check_array(const void* p, int64_t m, int64_t n, int64_t c, const char* what
 }
 
 }  // namespace
+
+namespace weno {
+int set_last_error(int code, const char* msg) {
+  g_err = msg;
+  return code;
+}
+}  // namespace weno
 
 extern "C" {
 

@@ -31,6 +31,7 @@ SIGNATURES = {
     "weno_l_local_workspace": (_sz, [_i64, _i64, _i]),
     "weno_l_local": (_i, [_vp, _i64, _i64, _i64, _i64, _i64, _i64, _d, _d, _i, _d, _d, _i, _i, _vp, _vp, _sz, _vp]),
     "weno_l_local_host": (_i, [_vp, _i64, _i64, _i64, _d, _d, _i, _d, _d, _i, _i, _vp]),
+    "weno_l_local_noalloc": (_i, [_vp, _i64, _i64, _i64, _i64, _i64, _i64, _d, _d, _i, _d, _d, _i, _i, _vp, _vp]),
     "weno_solver_create": (_i, [ctypes.POINTER(_vp), _i64, _i64, _d, _d, _i, _i, _i, _i, _d, _d, _d, _i, _i64, _vp,
                                 _vp]),
     "weno_solver_destroy": (_i, [_vp]),

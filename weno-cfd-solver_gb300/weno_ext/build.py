@@ -32,6 +32,7 @@ UNITS = {
     "tu_fast.cu": ["--fmad=true"],
     "capi.cu": [],
     "probe.cu": [],
+    "noalloc.cu": [],
 }
 
 
