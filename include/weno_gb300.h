@@ -157,6 +157,41 @@ int weno_solver_timing_report(weno_solver* s, double* ms, int64_t* launches, int
 /* Number of kernel launches one step enqueues (for launch accounting). */
 int weno_solver_launches_per_step(weno_solver* s);
 
+/* ------------------------------------------------------------------------
+ * Batched solver: many independent problems of uneven size stepped together.
+ * Each solve is the loop of weno_solver_* (same scheme, boundary kinds and
+ * per-solve dt = CFL*dx/(max(c+|u|)+1e-16) clipped to its own t_end), with
+ * only its interior cells stored in a packed pool of `pool_cells` cells per RK
+ * buffer.  One step of ALL active solves is five launches: the per-solve dt,
+ * three persistent stage kernels that walk a packed list of TX x TY tiles
+ * (tile shape `tile_config`, 0..weno_batch_tile_config_count()-1) and fuse
+ * the whole residual with the stage combination in shared memory, and the
+ * clock update; the boundary fill is applied while tiles load.  Solves can be
+ * added and removed between runs (continuous batching).  Results of a solve
+ * do not depend on the other solves in the batch.
+ * ---------------------------------------------------------------------- */
+typedef struct weno_batch weno_batch;
+
+int weno_batch_tile_config_count(void);
+int weno_batch_create(weno_batch** out, int64_t pool_cells, int max_solves, int precision, int mode, int cons,
+                      int force_hlle, double gamma, double jp_lo, double jp_hi, double cfl, int tile_config,
+                      void* stream);
+int weno_batch_destroy(weno_batch* b);
+/* Add a solve from a device array (nx+6, ny+6, c>=4) (ghost cells ignored);
+ * t_end < 0 for step-count only; max_steps <= 0 for no cap.  Returns its slot. */
+int weno_batch_add(weno_batch* b, int64_t nx, int64_t ny, double dx, int bc_kind, int64_t bound, const double* post8,
+                   double t_end, int64_t max_steps, const double* q, int64_t c, int64_t s0, int64_t s1, int64_t s2,
+                   int* slot_out);
+int weno_batch_remove(weno_batch* b, int slot);
+/* Enqueue nsteps steps of every active solve (finished solves are no-ops). */
+int weno_batch_run(weno_batch* b, int64_t nsteps, int use_graph);
+/* The driver's (nx+6, ny+6, 8) array of one solve (device pointer); synchronises. */
+int weno_batch_get_state(weno_batch* b, int slot, double* out);
+int weno_batch_info(weno_batch* b, int slot, double* t, int64_t* steps, int* active, int* status);
+/* Synchronise and copy every slot's active flag, time and step count (arrays of max_solves). */
+int weno_batch_poll(weno_batch* b, int* active, double* t, int64_t* steps);
+int weno_batch_stats(weno_batch* b, int64_t* ntiles, int64_t* free_cells, int* launches_per_step);
+
 /* Diagnostics: measured FP64 FMA (TFLOP/s), FP64 divide (per s) and FP32 FMA
  * (TFLOP/s) throughput of the current device -- the compute-roofline
  * denominators, with no counterpart in the reference. */

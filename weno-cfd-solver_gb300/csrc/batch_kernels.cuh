@@ -1,0 +1,484 @@
+// Batched solver: many independent 2-D problems of uneven size stepped together.
+//
+// Pool layout.  Every solve stores only its interior cells, as four conserved
+// planes of nx x ny (row stride ny, plane stride `ps`) at element offset `off`
+// of a packed pool; the pool exists three times (current state, stage 1,
+// stage 2) with identical offsets.  Ghost cells are never stored: a tile
+// loader resolves each ghost index to the interior cell (or inflow constant)
+// the boundary fill would have copied there (Rie_prob_2d_rs.py:123-152,
+// unitest.py:207-227), so the fill costs no pass of its own.
+//
+// Work.  The unit is a tile of TX x TY interior cells of one solve.  A packed
+// tile list (solve, i0, j0) covers every active solve; one persistent kernel
+// per RK stage walks it.  A CTA loads the tile plus its halo into shared
+// memory, runs pass 1 (normal WENO5), pass 2 (Gauss-quadrature WENO, fluxes,
+// Riemann solver), the sensor blend and the flux difference fused with the
+// SSP-RK3 stage combination, and writes the tile of the next stage state.
+// Stage 3 also reduces the new state's wave speed per solve for the next dt.
+#pragma once
+
+#include "euler_math.cuh"
+#include "step_ctl.h"
+
+namespace weno {
+
+struct SolveDesc {
+  long long off;  // element offset of plane 0 in each pool
+  long long ps;   // plane stride (elements)
+  int nx, ny;
+  int bc;         // 0 transmissive (mirror), 1 oblique-shock / DMR segments
+  int bound;      // DMR: last row of the inflow segment on the lower boundary
+  double dx;      // cell size (dx = dy)
+  double post[8]; // DMR inflow state: conserved channels 0..3, primitive channels 4..7
+};
+
+struct SolveCtl {
+  double t, t_end, dt, cfl_dx;
+  unsigned long long cmax_bits;
+  int active;      // 0: finished (t >= t_end - 1e-12 or step cap) or not admitted
+  int status;      // 1: non-finite wave speed
+  long long steps, max_steps;
+};
+
+inline namespace WENO_TU_NS {
+
+// Where the boundary fill would take ghost cell (I, J) (padded coordinates)
+// from: an interior cell (i, j) with a sign on the normal momentum, or the
+// inflow constant.
+struct GhostSrc {
+  int i, j;
+  bool post;
+  bool flip2;
+};
+
+__device__ __forceinline__ GhostSrc resolve_cell(const SolveDesc& d, int I, int J) {
+  GhostSrc g{0, 0, false, false};
+  const int nx = d.nx, ny = d.ny;
+  if (d.bc == 0) {
+    const int M = nx + 6, N = ny + 6;
+    const int si = I < 3 ? 5 - I : (I >= M - 3 ? 2 * M - 7 - I : I);
+    const int sj = J < 3 ? 5 - J : (J >= N - 3 ? 2 * N - 7 - J : J);
+    g.i = si - 3;
+    g.j = sj - 3;
+    return g;
+  }
+  if (I < 3) {
+    g.post = true;
+  } else if (J >= ny + 3) {
+    g.i = (I < nx + 3 ? I : nx + 2) - 3;
+    g.j = ny - 1;
+  } else if (J < 3) {
+    const int s = I < nx + 3 ? I : nx + 2;
+    const int band_row = (I >= nx + 3 && J < I - nx - 3) ? nx + 2 : I;
+    if (band_row <= d.bound) {
+      g.post = true;
+    } else if (band_row <= d.bound + 9) {
+      g.i = s - 3;
+      g.j = 0;
+    } else {
+      g.i = s - 3;
+      g.j = 2 - J;
+      g.flip2 = true;
+    }
+  } else if (I >= nx + 3) {
+    g.i = nx - 1;
+    g.j = J - 3;
+  } else {
+    g.i = I - 3;
+    g.j = J - 3;
+  }
+  return g;
+}
+
+template <int TX, int TY, bool BLEND>
+struct TileGeom {
+  static constexpr int HF = BLEND ? 1 : 0;     // extra face halo for the sensor stencil
+  static constexpr int UR = TX + 6 + 2 * HF;   // tile rows incl. halo
+  static constexpr int UC = TY + 6 + 2 * HF;
+  static constexpr int P1XR = TX + 1 + 2 * HF, P1XC = TY + 4 + 2 * HF;  // pass-1 x faces x columns
+  static constexpr int P1YR = TX + 4 + 2 * HF, P1YC = TY + 1 + 2 * HF;  // pass-1 rows x y faces
+  static constexpr int P1 = (P1XR * P1XC > P1YR * P1YC) ? P1XR * P1XC : P1YR * P1YC;
+  static constexpr int FXR = TX + 1 + 2 * HF, FXC = TY + 2 * HF;  // x faces for the residual (+sensor halo)
+  static constexpr int FYR = TX + 2 * HF, FYC = TY + 1 + 2 * HF;
+  static constexpr int NF = BLEND ? 9 : 4;    // HLLC[4], HLLE[4], pbar  |  F[4]
+  static constexpr int U_ELEMS = 4 * UR * UC;
+  static constexpr int P1_ELEMS = 8 * P1;
+  static constexpr int FX_ELEMS = NF * FXR * FXC;
+  static constexpr int FY_ELEMS = NF * FYR * FYC;
+  static constexpr int TOTAL = U_ELEMS + P1_ELEMS + FX_ELEMS + FY_ELEMS;
+};
+
+// Sensor weight at face (fr, fc) of a local face array of R x C entries whose
+// global origin is (gr0, gc0) in a global face array of GR x GC entries
+// (riemann.rs:352-410: central differences, one-sided on the global edges).
+template <class T, bool FAST>
+__device__ __forceinline__ T tile_sensor(const T* pbar, int R, int C, int fr, int fc, int gr, int gc, int GR, int GC,
+                                         T jp_lo, T jp_hi) {
+  const int min_dim = GR < GC ? GR : GC;
+  const T dx = T(1.0) / T((double)min_dim);
+  const T two_dx = T(2.0) * dx;
+  const int ra = gr == 0 ? 0 : (gr == GR - 1 ? -1 : -1);
+  const int rb = gr == 0 ? 1 : (gr == GR - 1 ? 0 : 1);
+  const int ca = gc == 0 ? 0 : (gc == GC - 1 ? -1 : -1);
+  const int cb = gc == 0 ? 1 : (gc == GC - 1 ? 0 : 1);
+  (void)R;
+  const T p = pbar[fr * C + fc];
+  const T dpdx = qdiv<T, FAST>(pbar[(fr + rb) * C + fc] - pbar[(fr + ra) * C + fc], two_dx);
+  const T dpdy = qdiv<T, FAST>(pbar[fr * C + fc + cb] - pbar[fr * C + fc + ca], two_dx);
+  return sensor_weight<T, FAST>(dpdx, dpdy, p, jp_lo, jp_hi);
+}
+
+// One SSP-RK3 stage (STAGE 1..3) for every tile of the list.  Qin is the stage
+// input pool (q, q1, q2), Qn the step's initial state, Qo the output pool.
+template <class T, bool FAST, bool CHAR, bool BLEND, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict__ solves, SolveCtl* ctl,
+                                                     const int4* __restrict__ tiles, int ntiles, const T* Qin,
+                                                     const T* Qn, T* Qo, int stage, T gamma, T jp_lo, T jp_hi) {
+  using G = TileGeom<TX, TY, BLEND>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* U = reinterpret_cast<T*>(smem_raw);
+  T* P1 = U + G::U_ELEMS;
+  T* FX = P1 + G::P1_ELEMS;
+  T* FY = FX + G::FX_ELEMS;
+  __shared__ double red[NT / 32];
+  const int tid = threadIdx.x;
+
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int4 tl = tiles[t];
+    const SolveDesc d = solves[tl.x];
+    if (!ctl[tl.x].active) continue;  // uniform across the CTA
+    const int i0 = tl.y, j0 = tl.z;
+    const int nx = d.nx, ny = d.ny;
+    const T* qin = Qin + d.off;
+    const long long ps = d.ps;
+    const int HF = G::HF;
+
+    // ---- load the tile and its halo, resolving ghost cells ----
+    for (int e = tid; e < G::UR * G::UC; e += NT) {
+      const int r = e / G::UC, c = e % G::UC;
+      const int I = i0 - HF + r, J = j0 - HF + c;  // padded coordinates
+      T v[4] = {T(0), T(0), T(0), T(0)};
+      if (I >= 0 && I < nx + 6 && J >= 0 && J < ny + 6) {
+        const GhostSrc g = resolve_cell(d, I, J);
+        if (g.post) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) v[k] = T(d.post[k]);
+        } else {
+          const long long o = (long long)g.i * ny + g.j;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) v[k] = qin[k * ps + o];
+          if (g.flip2) v[2] = -v[2];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) U[k * G::UR * G::UC + e] = v[k];
+    }
+    __syncthreads();
+
+    // ---- x sweep: pass 1 on faces fi = i0-HF+fr (global face rows 0..nx) ----
+    for (int e = tid; e < G::P1XR * G::P1XC; e += NT) {
+      const int fr = e / G::P1XC, c = e % G::P1XC;
+      const int fi = i0 - HF + fr;
+      if (fi < 0 || fi > nx) continue;
+      // pass-1 column J = j0+1-HF+c <-> tile column c+1
+      T cells[6][4];
+#pragma unroll
+      for (int s = 0; s < 6; ++s)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) cells[s][k] = U[k * G::UR * G::UC + (fr + s) * G::UC + c + 1];
+      T ql[4], qr[4];
+      pass1_face<T, FAST, false, CHAR>(cells, gamma, ql, qr);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        P1[k * G::P1 + e] = ql[k];
+        P1[(4 + k) * G::P1 + e] = qr[k];
+      }
+    }
+    __syncthreads();
+    // ---- x sweep: pass 2 on faces (fi, jj), jj = j0-HF+fc ----
+    for (int e = tid; e < G::FXR * G::FXC; e += NT) {
+      const int fr = e / G::FXC, fc = e % G::FXC;
+      const int fi = i0 - HF + fr, jj = j0 - HF + fc;
+      if (fi < 0 || fi > nx || jj < 0 || jj >= ny) continue;
+      T ql[4], qr[4], fl[4], fr_[4];
+      {
+        T a1[4], a2[4], f1[4], f2[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const T* p = P1 + k * G::P1 + fr * G::P1XC + fc;
+          weno5_gq_pair<T, FAST>(p[0], p[1], p[2], p[3], p[4], a1[k], a2[k]);
+        }
+        euler_flux<T, FAST, false>(a1, gamma, f1);
+        euler_flux<T, FAST, false>(a2, gamma, f2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          fl[k] = T(0.5) * (f1[k] + f2[k]);
+          ql[k] = T(0.5) * (a1[k] + a2[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const T* p = P1 + (4 + k) * G::P1 + fr * G::P1XC + fc;
+          weno5_gq_pair<T, FAST>(p[0], p[1], p[2], p[3], p[4], a1[k], a2[k]);
+        }
+        euler_flux<T, FAST, false>(a1, gamma, f1);
+        euler_flux<T, FAST, false>(a2, gamma, f2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          fr_[k] = T(0.5) * (f2[k] + f1[k]);
+          qr[k] = T(0.5) * (a1[k] + a2[k]);
+        }
+      }
+      const RiemannPre<T, FAST, false> rp = riemann_pre<T, FAST, false>(ql, qr, gamma);
+      T F[4];
+      hlle_flux<T, FAST, false>(rp, ql, fl, qr, fr_, F);
+      const int FN = G::FXR * G::FXC;
+      if constexpr (BLEND) {
+        T Gc[4];
+        hllc_flux<T, FAST, false>(rp, ql, fl, qr, fr_, Gc);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          FX[k * FN + e] = Gc[k];
+          FX[(4 + k) * FN + e] = F[k];
+        }
+        FX[8 * FN + e] = T(0.5) * (rp.p_l + rp.p_r);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) FX[k * FN + e] = F[k];
+      }
+    }
+    __syncthreads();
+
+    // ---- y sweep: pass 1 on rows I = i0+1-HF+r, faces fj = j0-HF+fc ----
+    for (int e = tid; e < G::P1YR * G::P1YC; e += NT) {
+      const int r = e / G::P1YC, fc = e % G::P1YC;
+      const int I = i0 + 1 - HF + r, fj = j0 - HF + fc;
+      if (I < 0 || I >= nx + 6 || fj < 0 || fj > ny) continue;
+      T cells[6][4];
+#pragma unroll
+      for (int s = 0; s < 6; ++s)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) cells[s][k] = U[k * G::UR * G::UC + (r + 1) * G::UC + fc + s];
+      T ql[4], qr[4];
+      pass1_face<T, FAST, true, CHAR>(cells, gamma, ql, qr);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        P1[k * G::P1 + e] = ql[k];
+        P1[(4 + k) * G::P1 + e] = qr[k];
+      }
+    }
+    __syncthreads();
+    // ---- y sweep: pass 2 on faces (ii, fj), ii = i0-HF+fr ----
+    for (int e = tid; e < G::FYR * G::FYC; e += NT) {
+      const int fr = e / G::FYC, fc = e % G::FYC;
+      const int ii = i0 - HF + fr, fj = j0 - HF + fc;
+      if (ii < 0 || ii >= nx || fj < 0 || fj > ny) continue;
+      T ql[4], qr[4], fl[4], fr_[4];
+      {
+        T a1[4], a2[4], f1[4], f2[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const T* p = P1 + k * G::P1 + fr * G::P1YC + fc;
+          weno5_gq_pair<T, FAST>(p[0], p[G::P1YC], p[2 * G::P1YC], p[3 * G::P1YC], p[4 * G::P1YC], a1[k], a2[k]);
+        }
+        euler_flux<T, FAST, true>(a1, gamma, f1);
+        euler_flux<T, FAST, true>(a2, gamma, f2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          fl[k] = T(0.5) * (f1[k] + f2[k]);
+          ql[k] = T(0.5) * (a1[k] + a2[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const T* p = P1 + (4 + k) * G::P1 + fr * G::P1YC + fc;
+          weno5_gq_pair<T, FAST>(p[0], p[G::P1YC], p[2 * G::P1YC], p[3 * G::P1YC], p[4 * G::P1YC], a1[k], a2[k]);
+        }
+        euler_flux<T, FAST, true>(a1, gamma, f1);
+        euler_flux<T, FAST, true>(a2, gamma, f2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          fr_[k] = T(0.5) * (f2[k] + f1[k]);
+          qr[k] = T(0.5) * (a1[k] + a2[k]);
+        }
+      }
+      const RiemannPre<T, FAST, true> rp = riemann_pre<T, FAST, true>(ql, qr, gamma);
+      T F[4];
+      hlle_flux<T, FAST, true>(rp, ql, fl, qr, fr_, F);
+      const int FN = G::FYR * G::FYC;
+      if constexpr (BLEND) {
+        T Gc[4];
+        hllc_flux<T, FAST, true>(rp, ql, fl, qr, fr_, Gc);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          FY[k * FN + e] = Gc[k];
+          FY[(4 + k) * FN + e] = F[k];
+        }
+        FY[8 * FN + e] = T(0.5) * (rp.p_l + rp.p_r);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) FY[k * FN + e] = F[k];
+      }
+    }
+    __syncthreads();
+
+    // ---- residual + SSP-RK3 combination (+ wave speed for the next dt) ----
+    const double dt = ctl[tl.x].dt;
+    const T* qn = Qn + d.off;
+    T* qo = Qo + d.off;
+    double best = 0.0;
+    bool bad = false;
+    for (int e = tid; e < TX * TY; e += NT) {
+      const int il = e / TY, jl = e % TY;
+      const int i = i0 + il, j = j0 + jl;
+      if (i >= nx || j >= ny) continue;
+      T L[4];
+      const int fxr = il + HF, fxc = jl + HF;  // Fx rows fi = i, i+1
+      const int fyr = il + HF, fyc = jl + HF;  // Fy cols fj = j, j+1
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        T fxa, fxb, fya, fyb;
+        if constexpr (BLEND) {
+          const int FN = G::FXR * G::FXC;
+          const T wa = tile_sensor<T, FAST>(FX + 8 * FN, G::FXR, G::FXC, fxr, fxc, i, j, nx + 1, ny, jp_lo, jp_hi);
+          const T wb = tile_sensor<T, FAST>(FX + 8 * FN, G::FXR, G::FXC, fxr + 1, fxc, i + 1, j, nx + 1, ny, jp_lo,
+                                            jp_hi);
+          fxa = wa * FX[k * FN + fxr * G::FXC + fxc] + (T(1.0) - wa) * FX[(4 + k) * FN + fxr * G::FXC + fxc];
+          fxb = wb * FX[k * FN + (fxr + 1) * G::FXC + fxc] + (T(1.0) - wb) * FX[(4 + k) * FN + (fxr + 1) * G::FXC + fxc];
+          const int FM = G::FYR * G::FYC;
+          const T va = tile_sensor<T, FAST>(FY + 8 * FM, G::FYR, G::FYC, fyr, fyc, i, j, nx, ny + 1, jp_lo, jp_hi);
+          const T vb = tile_sensor<T, FAST>(FY + 8 * FM, G::FYR, G::FYC, fyr, fyc + 1, i, j + 1, nx, ny + 1, jp_lo,
+                                            jp_hi);
+          fya = va * FY[k * FM + fyr * G::FYC + fyc] + (T(1.0) - va) * FY[(4 + k) * FM + fyr * G::FYC + fyc];
+          fyb = vb * FY[k * FM + fyr * G::FYC + fyc + 1] + (T(1.0) - vb) * FY[(4 + k) * FM + fyr * G::FYC + fyc + 1];
+        } else {
+          const int FN = G::FXR * G::FXC, FM = G::FYR * G::FYC;
+          fxa = FX[k * FN + fxr * G::FXC + fxc];
+          fxb = FX[k * FN + (fxr + 1) * G::FXC + fxc];
+          fya = FY[k * FM + fyr * G::FYC + fyc];
+          fyb = FY[k * FM + fyr * G::FYC + fyc + 1];
+        }
+        const T dfdx = (fxb - fxa) / T(d.dx);
+        const T dgdy = (fyb - fya) / T(d.dx);
+        L[k] = -(dfdx + dgdy);
+      }
+      const long long o = (long long)i * ny + j;
+      // stage input of this cell, from the tile (padded (i+3, j+3) -> tile (i+3-i0+HF, ...))
+      const int ur = i + 3 - i0 + HF, uc = j + 3 - j0 + HF;
+      T v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const T qs = U[k * G::UR * G::UC + ur * G::UC + uc];
+        if (stage == 1) {
+          v[k] = qs + T(dt) * L[k];
+        } else if (stage == 2) {
+          v[k] = T(0.75) * qn[k * ps + o] + T(0.25) * qs + T(0.25 * dt) * L[k];
+        } else {
+          v[k] = T(1.0 / 3.0) * qn[k * ps + o] + T(2.0 / 3.0) * qs + T((2.0 / 3.0) * dt) * L[k];
+        }
+        qo[k * ps + o] = v[k];
+      }
+      if (stage == 3) {
+        // Rie_prob_2d_rs.py:312-315 on the new state (primitives as con2primi writes them)
+        const double r0 = (double)v[0];
+        const double rho = fmax(r0, kEps);
+        const double uu = (double)v[1] / rho, vv = (double)v[2] / rho;
+        const double pp = fmax(((double)gamma - 1.0) * ((double)v[3] - 0.5 * rho * (uu * uu + vv * vv)), kEps);
+        const double x = sqrt((double)gamma * pp / fmax(r0, 1e-14)) + sqrt(uu * uu + vv * vv);
+        if (!(x >= 0.0) || isinf(x)) bad = true;
+        else best = fmax(best, x);
+      }
+    }
+    if (stage == 3) {
+      for (int off = 16; off > 0; off >>= 1) {
+        best = fmax(best, __shfl_xor_sync(0xffffffffu, best, off));
+        bad = __any_sync(0xffffffffu, bad);
+      }
+      if ((tid & 31) == 0) red[tid >> 5] = bad ? -1.0 : best;
+      __syncthreads();
+      if (tid == 0) {
+        double b = 0.0;
+        bool anybad = false;
+        for (int w = 0; w < NT / 32; ++w) {
+          if (red[w] < 0.0) anybad = true;
+          else b = fmax(b, red[w]);
+        }
+        atomicMax(&ctl[tl.x].cmax_bits, (unsigned long long)__double_as_longlong(b));
+        if (anybad) atomicOr(&ctl[tl.x].status, 1);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Wave-speed maximum of the current state per solve (the first dt of a run).
+template <class T, int NT>
+__global__ void __launch_bounds__(NT) k_cfl_tiles(const SolveDesc* __restrict__ solves, SolveCtl* ctl,
+                                                   const int4* __restrict__ tiles, int ntiles, int TX, int TY,
+                                                   const T* Q, T gamma) {
+  __shared__ double red[NT / 32];
+  const int tid = threadIdx.x;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int4 tl = tiles[t];
+    if (!ctl[tl.x].active) continue;
+    const SolveDesc d = solves[tl.x];
+    double best = 0.0;
+    bool bad = false;
+    for (int e = tid; e < TX * TY; e += NT) {
+      const int i = tl.y + e / TY, j = tl.z + e % TY;
+      if (i >= d.nx || j >= d.ny) continue;
+      const long long o = d.off + (long long)i * d.ny + j;
+      const double r0 = (double)Q[o];
+      const double rho = fmax(r0, kEps);
+      const double uu = (double)Q[o + d.ps] / rho, vv = (double)Q[o + 2 * d.ps] / rho;
+      const double pp = fmax(((double)gamma - 1.0) * ((double)Q[o + 3 * d.ps] - 0.5 * rho * (uu * uu + vv * vv)), kEps);
+      const double x = sqrt((double)gamma * pp / fmax(r0, 1e-14)) + sqrt(uu * uu + vv * vv);
+      if (!(x >= 0.0) || isinf(x)) bad = true;
+      else best = fmax(best, x);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      best = fmax(best, __shfl_xor_sync(0xffffffffu, best, off));
+      bad = __any_sync(0xffffffffu, bad);
+    }
+    if ((tid & 31) == 0) red[tid >> 5] = bad ? -1.0 : best;
+    __syncthreads();
+    if (tid == 0) {
+      double b = 0.0;
+      bool anybad = false;
+      for (int w = 0; w < NT / 32; ++w) {
+        if (red[w] < 0.0) anybad = true;
+        else b = fmax(b, red[w]);
+      }
+      atomicMax(&ctl[tl.x].cmax_bits, (unsigned long long)__double_as_longlong(b));
+      if (anybad) atomicOr(&ctl[tl.x].status, 1);
+    }
+    __syncthreads();
+  }
+}
+
+// Per-solve clock.  phase 0 (start of a step): dt from the reduced wave speed,
+// clipped to t_end.  phase 1 (end of a step): advance the clock, test the loop
+// condition, clear the reduction for the next step's dt.
+__global__ void k_solve_clock(SolveCtl* ctl, int nsolves, int phase) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsolves) return;
+  SolveCtl& c = ctl[s];
+  if (!c.active) return;
+  if (phase == 0) {
+    const double cmax = __longlong_as_double((long long)c.cmax_bits) + 1e-16;
+    double dt = c.cfl_dx / cmax;
+    if (c.t_end >= 0.0) {
+      const double remaining = c.t_end - c.t;
+      if (remaining < dt) dt = remaining;
+    }
+    c.dt = dt;
+    c.cmax_bits = 0ull;
+  } else {
+    c.t += c.dt;
+    c.steps += 1;
+    bool more = c.steps < c.max_steps;
+    if (c.t_end >= 0.0) more = more && (c.t < c.t_end - 1e-12);
+    c.active = more ? 1 : 0;
+  }
+}
+
+}  // inline namespace WENO_TU_NS
+}  // namespace weno

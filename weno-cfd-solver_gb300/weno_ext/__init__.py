@@ -34,7 +34,7 @@ from ._lib import WenoError
 __all__ = [
     "flux_x_py", "flux_y_py", "con2primi_py", "weno_x_py", "weno_y_py", "hllc_x_rs_py", "hllc_y_rs_py",
     "hlle_x_rs_py", "hlle_y_rs_py", "hllc_hlle_x_rs_py", "hllc_hlle_y_rs_py", "l_local_py",
-    "set_mode", "get_mode", "Solver", "WenoError", "library_path",
+    "set_mode", "get_mode", "Solver", "Batch", "WenoError", "library_path",
 ]
 
 _MODE = _lib.FAST if os.environ.get("WENO_EXT_MODE", "exact").lower() == "fast" else _lib.EXACT
@@ -255,3 +255,4 @@ def l_local_py(u, dx, gamma, force_hlle, jp_cri, cons_switch=False):
 
 
 from .solver import Solver  # noqa: E402
+from .batch import Batch  # noqa: E402

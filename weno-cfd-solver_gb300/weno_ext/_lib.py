@@ -45,6 +45,18 @@ SIGNATURES = {
     "weno_solver_timing_report": (_i, [_vp, ctypes.POINTER(_d), ctypes.POINTER(_i64), _i]),
     "weno_solver_launches_per_step": (_i, [_vp]),
     "weno_probe_rates": (_i, [ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d), _vp]),
+    "weno_batch_tile_config_count": (_i, []),
+    "weno_batch_create": (_i, [ctypes.POINTER(_vp), _i64, _i, _i, _i, _i, _i, _d, _d, _d, _d, _i, _vp]),
+    "weno_batch_destroy": (_i, [_vp]),
+    "weno_batch_add": (_i, [_vp, _i64, _i64, _d, _i, _i64, _vp, _d, _i64, _vp, _i64, _i64, _i64, _i64,
+                            ctypes.POINTER(_i)]),
+    "weno_batch_remove": (_i, [_vp, _i]),
+    "weno_batch_run": (_i, [_vp, _i64, _i]),
+    "weno_batch_get_state": (_i, [_vp, _i, _vp]),
+    "weno_batch_info": (_i, [_vp, _i, ctypes.POINTER(_d), ctypes.POINTER(_i64), ctypes.POINTER(_i),
+                             ctypes.POINTER(_i)]),
+    "weno_batch_poll": (_i, [_vp, _vp, _vp, _vp]),
+    "weno_batch_stats": (_i, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i)]),
 }
 
 _lib = None

@@ -33,6 +33,10 @@ UNITS = {
     "capi.cu": [],
     "probe.cu": [],
     "noalloc.cu": [],
+    "batch.cu": ["--fmad=false"],
+    "batch_exact.cu": ["--fmad=false"],
+    "batch_f64.cu": ["--fmad=true"],
+    "batch_f32.cu": ["--fmad=true"],
 }
 
 
