@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -183,6 +184,178 @@ def run_reference(args):
     return 0
 
 
+def _l1_linf(a, b):
+    out = {}
+    for k, nm in enumerate(("rho", "rho_u", "rho_v", "E")):
+        x, y = a[3:-3, 3:-3, k], b[3:-3, 3:-3, k]
+        den = np.abs(y).sum()
+        out[nm] = {"rel_l1": float(np.abs(x - y).sum() / den) if den else None,
+                   "linf": float(np.abs(x - y).max()),
+                   "rel_linf": float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300))}
+    return out
+
+
+def run_accuracy(args):
+    """c1: 2048^2 four-quadrant, char-WENO5 + GQ + HLLE, CFL 0.45, 500 steps in FP64
+    exact (bit-identical to the reference arithmetic), FP64 fast and FP32; L1/Linf of
+    FP32 and fast against exact.  c2: oblique shock 4096x1024 on [0,4]x[0,1], seeded
+    Mach ~ U[2,10], angle ~ U[30,75] deg, char-WENO5 + HLLC (blend 1e4/1.1e4), CFL 0.1,
+    1000 steps, FP32 bulk (FP64 dt, positivity check, conservation sums) against FP64."""
+    import torch
+    torch.cuda.set_device(0)
+    import weno_ext
+    from weno_ext import problems
+    # The configurations name the characteristic-wise reconstruction.  With the
+    # reference's eigenvector matrices (L*R != I off rho = 1) that scheme produces
+    # NaN on these problems in every precision, the exact one included, so the
+    # accuracy runs use the component-wise reconstruction and the characteristic
+    # runs report the first step at which the reference algorithm turns non-finite.
+    recon = os.environ.get("WENO_ACC_RECON", "cons")
+    cons = recon == "cons"
+    if args.config == "c1":
+        nx, ny, nsteps = 2048, 2048, int(os.environ.get("WENO_C1_STEPS", "500"))
+        q0 = problems.quadrant(nx, ny, seed=SEED + 1)
+        kw = dict(cons=cons, force_hlle=True, jp_cri=(0.2, 1.0), cfl=0.45)
+        runs = (("fp64_exact", 64, "exact"), ("fp64_fast", 64, "fast"), ("fp32", 32, "fast"))
+        dx, extra = 1.0 / 2048, {}
+        desc = f"four-quadrant Riemann {nx}x{ny}, {recon}-WENO5+GQ+HLLE, CFL 0.45, {nsteps} steps"
+        char_kw = dict(kw, cons=False)
+    else:
+        nx, ny, nsteps = 4096, 1024, int(os.environ.get("WENO_C2_STEPS", "1000"))
+        rng = np.random.default_rng(SEED + 2)
+        mach, theta = float(rng.uniform(2, 10)), math.radians(float(rng.uniform(30, 75)))
+        q0, bound, post = problems.oblique_shock(nx, ny, 4.0, 1.0, mach, theta)
+        kw = dict(cons=cons, force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.1, bc="dmr", bound=bound, post=post)
+        runs = (("fp64_fast", 64, "fast"), ("fp32", 32, "fast"))
+        dx, extra = 1.0 / 1024, {"mach": mach, "theta_deg": math.degrees(theta), "bound": bound}
+        desc = (f"oblique shock {nx}x{ny} on [0,4]x[0,1], M={mach:.3f}, angle={math.degrees(theta):.2f} deg, "
+                f"{recon}-WENO5+GQ+HLLC(blend 1e4/1.1e4), CFL 0.1, {nsteps} steps")
+        char_kw = dict(kw, cons=False)
+    # first non-finite step of the characteristic scheme (exact FP64 = the reference's arithmetic)
+    sc = weno_ext.Solver(nx, ny, dx, GAMMA, precision=64, mode="exact" if args.config == "c1" else "fast", **char_kw)
+    sc.set_state(q0)
+    blow = None
+    for k in range(0, nsteps, 5):
+        sc.run(5)
+        if sc.info()[2] & 1:
+            blow = sc.info()[1]
+            break
+    sc.close()
+    extra["characteristic_first_nonfinite_step"] = blow
+    res, states = {}, {}
+    for name, prec, mode in runs:
+        s = weno_ext.Solver(nx, ny, dx, GAMMA, precision=prec, mode=mode, **kw)
+        s.set_state(q0)
+        tot0 = s.totals()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s.stream)
+        s.run(nsteps)
+        e1.record(s.stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        t, k, st = s.info()
+        tot1 = s.totals()
+        states[name] = s.state()
+        res[name] = {"steps": k, "t": t, "status": st, "ms_per_step": ms / nsteps,
+                     "cell_updates_per_s": nx * ny * k / (ms / 1e3), "totals_start": tot0, "totals_end": tot1,
+                     "nan": bool(np.isnan(states[name]).any())}
+        s.close()
+    ref = "fp64_exact" if "fp64_exact" in states else "fp64_fast"
+    errors = {name: _l1_linf(states[name], states[ref]) for name in states if name != ref}
+    line = {"metric": "accuracy and cell-updates/s", "config_name": args.config, "unit": UNIT, "n_gpus": 1,
+            "data": "synthetic", "config": dict({"workload": desc}, **extra), "runs": res,
+            "errors_vs_" + ref: errors}
+    print(json.dumps(line))
+    return 0
+
+
+def run_c3(args):
+    """Batched: independent four-quadrant solves of uneven size (edges log-uniform in
+    [64, 1024], aspect <= 4), each with its own dt and t_end ~ U[0.1, 0.3], component
+    WENO5 + HLLC (blend thresholds 1e4 / 1.1e4), FP32, CFL 0.5, all advanced together by
+    graph-replayed steps of the persistent tile kernels; the tile shape is autotuned."""
+    import torch
+    torch.cuda.set_device(0)
+    import weno_ext
+    from weno_ext import autotune, problems
+    rng = np.random.default_rng(SEED + 3)
+    shapes = problems.batch_shapes(args.solves, 64, 1024, SEED + 3)
+    states = [(problems.quadrant(nx, ny, seed=SEED + k), 1.0 / max(nx, ny)) for k, (nx, ny) in enumerate(shapes)]
+    t_ends = rng.uniform(0.1, 0.3, len(shapes))
+    kw = dict(precision=32, mode="fast", cons=True, force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.5)
+    sample = states[:: max(1, len(states) // 64)]
+    cfg, tune = autotune.best_tile_config(sample, **kw)
+    cells = sum(nx * ny for nx, ny in shapes)
+    b = weno_ext.Batch(cells + 64 * len(shapes) + 4096, len(shapes), tile_config=cfg, **kw)
+    slots = [b.add(q, dx, t_end=float(te)) for (q, dx), te in zip(states, t_ends)]
+    b.run(1)
+    b.synchronize()
+    done_before = b.poll()[2].copy()
+    chunk = 20
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(b.stream)
+    graph_steps = 0
+    while True:
+        b.run(chunk)
+        graph_steps += chunk
+        act, tt, nn = b.poll()
+        if not act.any():
+            break
+    e1.record(b.stream)
+    e1.synchronize()
+    wall = time.perf_counter() - t0
+    ms = e0.elapsed_time(e1)
+    act, tt, nn = b.poll()
+    cu = int(sum(nx * ny * (int(n) - int(d)) for (nx, ny), n, d in zip(shapes, nn, done_before)))
+    st = b.stats()
+    line = {
+        "metric": "aggregate cell-updates/s, batched uneven four-quadrant solves (FP32)", "config_name": "c3",
+        "value": cu / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{len(shapes)} four-quadrant solves, edges log-uniform [64,1024], aspect<=4, "
+                               "cons-WENO5+GQ+HLLC, FP32, CFL 0.5, t_end~U[0.1,0.3], per-solve dt",
+                   "cells": cells, "tiles": st["tiles"], "tile_config": cfg, "autotune_ms_per_step": tune},
+        "steps_replayed": graph_steps, "cell_updates": cu, "gpu_ms": ms, "wall_s": wall,
+        "launches_per_step": st["launches_per_step"],
+        "max_steps_of_a_solve": int(nn.max()), "min_steps_of_a_solve": int(nn.min()),
+        "t_end_reached": bool(np.all(np.abs(tt - t_ends) < 1e-9)),
+    }
+    print(json.dumps(line))
+    b.close()
+    return 0
+
+
+def run_c4(args):
+    """Serving: a seeded Poisson stream of requests (quadrant or oblique-shock initial
+    data, FP32 or FP64 tag, seeded t_end) under an HBM budget with continuous batching."""
+    import torch
+    torch.cuda.set_device(0)
+    from weno_ext import serving
+    lo, hi = int(os.environ.get("WENO_C4_LO", "128")), int(os.environ.get("WENO_C4_HI", "512"))
+    rate = float(os.environ.get("WENO_C4_RATE", "40"))
+    t_end = (float(os.environ.get("WENO_C4_TLO", "0.02")), float(os.environ.get("WENO_C4_THI", "0.06")))
+    budget = int(float(os.environ.get("WENO_C4_BUDGET_GB", "150")) * 1e9)
+    reqs = serving.poisson_stream(args.requests, rate=rate, lo=lo, hi=hi, seed=SEED + 4, fp64_fraction=0.25,
+                                  t_end=t_end, shock_fraction=0.3)
+    srv = serving.Server(budget, fp64_share=0.5, max_solves=1024, steps_per_iter=8)
+    t0 = time.perf_counter()
+    srv.serve(reqs, realtime=True)
+    wall = time.perf_counter() - t0
+    srv.close()
+    summ = serving.summarize(reqs, wall)
+    line = {"metric": "p50/p99 time-to-solution and aggregate cell-updates/s, serving stream", "config_name": "c4",
+            "value": summ["aggregate_cell_updates_per_s"], "unit": UNIT, "n_gpus": 1, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": f"{args.requests} Poisson requests at {rate}/s, edges log-uniform [{lo},{hi}], "
+                                   f"t_end~U{t_end}, 25% FP64, 30% oblique shock, HBM budget {budget/1e9:.0f} GB",
+                       "steps_per_iteration": 8},
+            "serving": summ}
+    print(json.dumps(line))
+    return 0
+
+
 def time_solver(Solver, q0, nx, ny, steps, warmup, **kw):
     """Device-resident run; returns (ms for `steps` timed steps, solver)."""
     import torch
@@ -211,10 +384,21 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", default="headline", choices=["headline", "c1", "c2", "c3", "c4"],
+                    help="headline: the 4096^2 FP64 step (default); c1: 2048^2 FP64/FP32 accuracy run; "
+                         "c2: oblique shock 4096x1024 FP32 vs FP64; c3: batched uneven solves; c4: serving stream")
+    ap.add_argument("--solves", type=int, default=512)
+    ap.add_argument("--requests", type=int, default=300)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.config in ("c1", "c2"):
+        return run_accuracy(args)
+    if args.config == "c3":
+        return run_c3(args)
+    if args.config == "c4":
+        return run_c4(args)
 
     import torch
     world, rank, local = dist_setup()

@@ -144,9 +144,12 @@ int weno_solver_run(weno_solver* s, int64_t nsteps, double t_final, int use_grap
  * sync (rho_safe, u, v, p), then the boundary fill on all eight channels. */
 int weno_solver_get_state(weno_solver* s, double* out);
 int weno_solver_get_state_host(weno_solver* s, double* out);
-/* Synchronise and read the clock: simulated time, completed steps, status
- * (0 ok, else WENO_ERR_NUMERIC). */
+/* Synchronise and read the clock: simulated time, completed steps and the
+ * status bits seen so far (0 ok; 1 a non-finite wave speed; 2 a non-positive
+ * recovered density or pressure, checked in FP64 at every CFL reduction). */
 int weno_solver_info(weno_solver* s, double* t, int64_t* steps, int* status);
+/* FP64 sums of the four conserved variables over the interior (synchronises). */
+int weno_solver_totals(weno_solver* s, double* out4);
 /* CUDA-event timing of kernel groups, recorded on the solver's stream during
  * runs with use_graph=0.  Classes: 0 CFL reduction + dt, 1 boundary fills,
  * 2 x pass 1, 3 x pass 2, 4 sensor blends, 5 y pass 1, 6 y pass 2,
@@ -178,10 +181,11 @@ int weno_batch_create(weno_batch** out, int64_t pool_cells, int max_solves, int 
                       void* stream);
 int weno_batch_destroy(weno_batch* b);
 /* Add a solve from a device array (nx+6, ny+6, c>=4) (ghost cells ignored);
- * t_end < 0 for step-count only; max_steps <= 0 for no cap.  Returns its slot. */
+ * t_end < 0 for step-count only; max_steps <= 0 for no cap; cfl <= 0 takes the
+ * batch's CFL number.  Returns its slot. */
 int weno_batch_add(weno_batch* b, int64_t nx, int64_t ny, double dx, int bc_kind, int64_t bound, const double* post8,
-                   double t_end, int64_t max_steps, const double* q, int64_t c, int64_t s0, int64_t s1, int64_t s2,
-                   int* slot_out);
+                   double t_end, int64_t max_steps, double cfl, const double* q, int64_t c, int64_t s0, int64_t s1,
+                   int64_t s2, int* slot_out);
 int weno_batch_remove(weno_batch* b, int slot);
 /* Enqueue nsteps steps of every active solve (finished solves are no-ops). */
 int weno_batch_run(weno_batch* b, int64_t nsteps, int use_graph);

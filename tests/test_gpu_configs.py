@@ -1,0 +1,96 @@
+"""Full-size parity runs of the benchmark configurations that the oracle can finish
+in seconds, and size-independent properties of the larger ones."""
+
+import numpy as np
+import pytest
+
+from states import rel_l1
+
+pytestmark = pytest.mark.gpu
+G = 1.4
+
+
+def test_c0_full_run_matches_oracle(wx, orc):
+    """256^2 four-quadrant, component WENO5 + HLLC (blend 1e4/1.1e4), CFL 0.5, 200
+    steps, FP64: exact mode bit-identical to the oracle after the whole run, fast mode
+    within 1e-10 relative L1 per conserved variable.  (The WENO epsilon is the
+    reference's hard-coded 1e-12.)"""
+    from weno_ext import problems
+    n, steps = 256, 200
+    q0 = problems.quadrant(n, n, seed=20261200)
+    orc.set_threads(0)
+    ref = q0.copy()
+    for _ in range(steps):
+        dt = 0.5 / n / orc.cfl_cmax(ref, n, n, G)
+        orc.rk3_step(ref, n, n, 1.0 / n, dt, G, False, (1e4, 1.1e4), True)
+    for mode in ("exact", "fast"):
+        s = wx.Solver(n, n, 1.0 / n, G, mode=mode, cons=True, force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.5)
+        s.set_state(q0)
+        s.run(steps)
+        got = s.state()
+        assert s.steps == steps
+        if mode == "exact":
+            assert np.array_equal(got, ref)
+        else:
+            for k in range(4):
+                assert rel_l1(got[3:-3, 3:-3, k], ref[3:-3, 3:-3, k]) <= 1e-10
+
+
+def test_free_stream_preserved_at_4096(wx):
+    """A uniform state stays uniform to the last bit at the headline size."""
+    n = 4096
+    q = np.zeros((n + 6, n + 6, 8))
+    rho, u, v, p = 1.3, 0.4, -0.2, 0.9
+    q[..., 0], q[..., 1], q[..., 2] = rho, rho * u, rho * v
+    q[..., 3] = p / 0.4 + 0.5 * rho * (u * u + v * v)
+    q[..., 4], q[..., 5], q[..., 6], q[..., 7] = rho, u, v, p
+    for mode in ("exact", "fast"):
+        s = wx.Solver(n, n, 1.0 / n, G, mode=mode, cons=False, force_hlle=True, cfl=0.45)
+        s.set_state(q)
+        s.run(2)
+        got = s.state()
+        for k in range(4):
+            assert np.abs(got[..., k] - q[..., k]).max() <= 1e-13 * abs(q[0, 0, k]) + 1e-300
+        s.close()
+
+
+def test_mirror_symmetry_at_2048(wx):
+    """A state symmetric under x<->y (with u<->v) stays symmetric: the x and y sweeps
+    are exact transposes of each other."""
+    from weno_ext import problems
+    n = 2048
+    q = problems.quadrant(n, n, seed=3)
+    # symmetrise: q(i, j) = swap(q(j, i))
+    t = q.transpose(1, 0, 2)[:, :, [0, 2, 1, 3, 4, 6, 5, 7]]
+    upper = np.triu(np.ones((n + 6, n + 6), dtype=bool))
+    q = np.where(upper[..., None], q, t)
+    d = np.arange(n + 6)
+    for a, b in ((1, 2), (5, 6)):  # diagonal cells are their own mirror images: equal x/y components
+        m = 0.5 * (q[d, d, a] + q[d, d, b])
+        q[d, d, a] = m
+        q[d, d, b] = m
+    for mode in ("exact", "fast"):
+        s = wx.Solver(n, n, 1.0 / n, G, mode=mode, cons=False, force_hlle=True, cfl=0.45)
+        s.set_state(q)
+        s.run(3)
+        got = s.state()
+        back = got.transpose(1, 0, 2)[:, :, [0, 2, 1, 3, 4, 6, 5, 7]]
+        assert np.abs(back - got).max() <= 1e-12 * np.abs(got).max()
+        s.close()
+
+
+def test_fast_tracks_exact_at_2048(wx):
+    """The fast arithmetic stays within 1e-10 relative L1 of the exact (oracle-identical)
+    path over 20 steps at 2048^2, component-wise + HLLE."""
+    from weno_ext import problems
+    n = 2048
+    q = problems.quadrant(n, n, seed=4)
+    out = {}
+    for mode in ("exact", "fast"):
+        s = wx.Solver(n, n, 1.0 / n, G, mode=mode, cons=True, force_hlle=True, cfl=0.45)
+        s.set_state(q)
+        s.run(20)
+        out[mode] = s.state()
+        s.close()
+    for k in range(4):
+        assert rel_l1(out["fast"][3:-3, 3:-3, k], out["exact"][3:-3, 3:-3, k]) <= 1e-10

@@ -1,0 +1,82 @@
+"""Serving loop: continuous batching with HBM-footprint admission.  Each result must
+be bit-identical alone and in the mix; admission never exceeds the budget; a request
+with non-finite initial data finishes with a numeric status without disturbing the
+others; a request larger than its pool is refused up front."""
+
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _alone(wx, r):
+    from weno_ext import serving
+    solo = serving.Request(**{k: getattr(r, k) for k in ("rid", "arrival", "nx", "ny", "kind", "precision", "t_end",
+                                                         "seed", "mach", "theta", "init")})
+    solo.arrival = 0.0
+    srv = serving.Server(64 << 20, max_solves=4, steps_per_iter=3, keep_results=True)
+    srv.serve([solo], realtime=False, max_wall=120)
+    srv.close()
+    return solo
+
+
+def test_stream_results_equal_alone(wx):
+    from weno_ext import serving
+    reqs = serving.poisson_stream(14, rate=400.0, lo=24, hi=72, seed=5, fp64_fraction=0.3, t_end=(0.01, 0.03),
+                                  shock_fraction=0.3)
+    budget = 3 << 20  # small: forces requests to wait for space
+    srv = serving.Server(budget, max_solves=16, steps_per_iter=4, keep_results=True)
+    peak = {32: 0, 64: 0}
+
+    cells = {p: srv.budget[p] // (3 * 4 * (4 if p == 32 else 8)) for p in srv.pools}
+
+    def watch(it, now):
+        for p, b in srv.pools.items():
+            peak[p] = max(peak[p], cells[p] - b.stats()["free_cells"])
+
+    srv.serve(reqs, realtime=False, on_iteration=watch, max_wall=300)
+    srv.close()
+    assert all(r.status == 0 and r.finished >= r.arrival for r in reqs)
+    assert all(abs(r.t - r.t_end) < 1e-9 for r in reqs)
+    assert any(r.admitted > r.arrival for r in reqs)  # some had to wait
+    for p in peak:
+        assert 0 < peak[p] <= cells[p] + 16  # the pool is the budget (capacity rounded up to 64 elements)
+    summary = serving.summarize(reqs, max(r.finished for r in reqs))
+    assert summary["failed"] == 0 and summary["p99_s"] >= summary["p50_s"]
+    for r in (reqs[0], reqs[5], reqs[-1]):
+        solo = _alone(wx, r)
+        assert solo.steps == r.steps and solo.t == r.t
+        assert np.array_equal(solo.result, r.result)
+
+
+def test_nan_request_fails_alone(wx):
+    from weno_ext import problems, serving
+    good = serving.Request(rid=0, arrival=0.0, nx=40, ny=40, kind="quadrant", precision=32, t_end=0.02, seed=1)
+    q = problems.quadrant(40, 40, seed=2)
+    q[20, 20, 0] = float("nan")
+    bad = serving.Request(rid=1, arrival=0.0, nx=40, ny=40, kind="quadrant", precision=32, t_end=0.02, init=q)
+    srv = serving.Server(16 << 20, max_solves=4, steps_per_iter=4, keep_results=True)
+    srv.serve([good, bad], realtime=False, max_wall=120)
+    srv.close()
+    assert good.status == 0 and bad.status != 0
+    solo = _alone(wx, good)
+    assert np.array_equal(solo.result, good.result)
+
+
+def test_oversized_request_is_refused(wx):
+    from weno_ext import serving
+    r = serving.Request(rid=0, arrival=0.0, nx=512, ny=512, kind="quadrant", precision=64, t_end=0.01)
+    srv = serving.Server(8 << 20, max_solves=2)
+    with pytest.raises(ValueError):
+        srv.serve([r], realtime=False)
+    srv.close()
+
+
+def test_rankine_hugoniot_matches_the_reference_dmr_state():
+    from weno_ext import problems
+    rho, u, v, p = problems.rankine_hugoniot(10.0, math.pi / 3)
+    assert abs(rho - 8.0) < 1e-12 and abs(p - 116.5) < 1e-12
+    # the speed behind the shock is the reference's 8.25 (unitest.py:194-197)
+    assert abs(math.hypot(u, v) - 8.25) < 1e-12

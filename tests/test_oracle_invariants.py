@@ -102,3 +102,28 @@ def test_flop_tally_is_stable(orc):
             assert t["div"] > 0 and t["sqrt"] > 0
     # characteristic reconstruction costs more than component-wise
     assert per[(False, True)] > per[(True, True)]
+
+
+def test_reference_characteristic_scheme_is_unstable_on_low_density_quadrants(orc):
+    """With the reference's eigenvectors (L*R != I off rho = 1) the characteristic
+    reconstruction is not consistent, and on four-quadrant data with a rho ~ 0.11
+    quadrant the reference algorithm produces NaN within a few steps at CFL 0.5, while
+    the component-wise reconstruction and CFL 0.1 stay finite.  The GPU exact path
+    reproduces this bit for bit (tests/test_gpu_solver.py)."""
+    from states import quadrant
+    q = quadrant(np.random.default_rng(9), 40, 56)
+    orc.bc_transmissive(q)
+    orc.sync_primitives(q, G)
+
+    def first_nan(cfl, cons, steps=12):
+        qq = q.copy()
+        for k in range(steps):
+            dt = cfl / 56 / orc.cfl_cmax(qq, 40, 56, G)
+            orc.rk3_step(qq, 40, 56, 1 / 56, dt, G, True, (1e4, 1.1e4), cons)
+            if np.isnan(qq).any():
+                return k + 1
+        return None
+
+    assert first_nan(0.5, False) is not None and first_nan(0.5, False) <= 3
+    assert first_nan(0.5, True) is None
+    assert first_nan(0.1, False) is None

@@ -306,8 +306,8 @@ int weno_batch_destroy(weno_batch* b) {
 }
 
 int weno_batch_add(weno_batch* b, int64_t nx, int64_t ny, double dx, int bc_kind, int64_t bound, const double* post8,
-                   double t_end, int64_t max_steps, const double* q, int64_t c, int64_t s0, int64_t s1, int64_t s2,
-                   int* slot_out) {
+                   double t_end, int64_t max_steps, double cfl, const double* q, int64_t c, int64_t s0, int64_t s1,
+                   int64_t s2, int* slot_out) {
   if (!b || !q || !slot_out) return bfail(WENO_ERR_ARG, "batch_add: null argument");
   if (nx < 3 || ny < 3) return bfail(WENO_ERR_SHAPE, "batch_add: nx, ny >= 3 required");
   if (b->blend && (nx < 2 || ny < 2)) return bfail(WENO_ERR_SHAPE, "batch_add: grid too small for the sensor");
@@ -352,7 +352,7 @@ int weno_batch_add(weno_batch* b, int64_t nx, int64_t ny, double dx, int bc_kind
   WB_CK(cudaStreamSynchronize(b->stream));
   std::memset(&cc, 0, sizeof(SolveCtl));
   cc.t_end = t_end;
-  cc.cfl_dx = b->cfl * dx;
+  cc.cfl_dx = (cfl > 0.0 ? cfl : b->cfl) * dx;
   cc.active = 1;
   cc.max_steps = max_steps > 0 ? max_steps : (1ll << 62);
   WB_CK(cudaMemcpyAsync(b->d_ctl + slot, &cc, sizeof(SolveCtl), cudaMemcpyHostToDevice, b->stream));

@@ -45,6 +45,10 @@ inline namespace WENO_TU_NS {
 // Where the boundary fill would take ghost cell (I, J) (padded coordinates)
 // from: an interior cell (i, j) with a sign on the normal momentum, or the
 // inflow constant.
+__device__ __forceinline__ double nan_max_b(double a, double b) {
+  return (a != a || b != b) ? __longlong_as_double(0x7ff8000000000000ll) : fmax(a, b);
+}
+
 struct GhostSrc {
   int i, j;
   bool post;
@@ -325,7 +329,6 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
     const T* qn = Qn + d.off;
     T* qo = Qo + d.off;
     double best = 0.0;
-    bool bad = false;
     for (int e = tid; e < TX * TY; e += NT) {
       const int il = e / TY, jl = e % TY;
       const int i = i0 + il, j = j0 + jl;
@@ -383,26 +386,18 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
         const double uu = (double)v[1] / rho, vv = (double)v[2] / rho;
         const double pp = fmax(((double)gamma - 1.0) * ((double)v[3] - 0.5 * rho * (uu * uu + vv * vv)), kEps);
         const double x = sqrt((double)gamma * pp / fmax(r0, 1e-14)) + sqrt(uu * uu + vv * vv);
-        if (!(x >= 0.0) || isinf(x)) bad = true;
-        else best = fmax(best, x);
+        best = nan_max_b(best, x);
       }
     }
     if (stage == 3) {
-      for (int off = 16; off > 0; off >>= 1) {
-        best = fmax(best, __shfl_xor_sync(0xffffffffu, best, off));
-        bad = __any_sync(0xffffffffu, bad);
-      }
-      if ((tid & 31) == 0) red[tid >> 5] = bad ? -1.0 : best;
+      for (int off = 16; off > 0; off >>= 1) best = nan_max_b(best, __shfl_xor_sync(0xffffffffu, best, off));
+      if ((tid & 31) == 0) red[tid >> 5] = best;
       __syncthreads();
       if (tid == 0) {
         double b = 0.0;
-        bool anybad = false;
-        for (int w = 0; w < NT / 32; ++w) {
-          if (red[w] < 0.0) anybad = true;
-          else b = fmax(b, red[w]);
-        }
+        for (int w = 0; w < NT / 32; ++w) b = nan_max_b(b, red[w]);
         atomicMax(&ctl[tl.x].cmax_bits, (unsigned long long)__double_as_longlong(b));
-        if (anybad) atomicOr(&ctl[tl.x].status, 1);
+        if (!(b < INFINITY)) atomicOr(&ctl[tl.x].status, 1);
       }
     }
     __syncthreads();
@@ -421,7 +416,6 @@ __global__ void __launch_bounds__(NT) k_cfl_tiles(const SolveDesc* __restrict__ 
     if (!ctl[tl.x].active) continue;
     const SolveDesc d = solves[tl.x];
     double best = 0.0;
-    bool bad = false;
     for (int e = tid; e < TX * TY; e += NT) {
       const int i = tl.y + e / TY, j = tl.z + e % TY;
       if (i >= d.nx || j >= d.ny) continue;
@@ -431,24 +425,16 @@ __global__ void __launch_bounds__(NT) k_cfl_tiles(const SolveDesc* __restrict__ 
       const double uu = (double)Q[o + d.ps] / rho, vv = (double)Q[o + 2 * d.ps] / rho;
       const double pp = fmax(((double)gamma - 1.0) * ((double)Q[o + 3 * d.ps] - 0.5 * rho * (uu * uu + vv * vv)), kEps);
       const double x = sqrt((double)gamma * pp / fmax(r0, 1e-14)) + sqrt(uu * uu + vv * vv);
-      if (!(x >= 0.0) || isinf(x)) bad = true;
-      else best = fmax(best, x);
+      best = nan_max_b(best, x);
     }
-    for (int off = 16; off > 0; off >>= 1) {
-      best = fmax(best, __shfl_xor_sync(0xffffffffu, best, off));
-      bad = __any_sync(0xffffffffu, bad);
-    }
-    if ((tid & 31) == 0) red[tid >> 5] = bad ? -1.0 : best;
+    for (int off = 16; off > 0; off >>= 1) best = nan_max_b(best, __shfl_xor_sync(0xffffffffu, best, off));
+    if ((tid & 31) == 0) red[tid >> 5] = best;
     __syncthreads();
     if (tid == 0) {
       double b = 0.0;
-      bool anybad = false;
-      for (int w = 0; w < NT / 32; ++w) {
-        if (red[w] < 0.0) anybad = true;
-        else b = fmax(b, red[w]);
-      }
+      for (int w = 0; w < NT / 32; ++w) b = nan_max_b(b, red[w]);
       atomicMax(&ctl[tl.x].cmax_bits, (unsigned long long)__double_as_longlong(b));
-      if (anybad) atomicOr(&ctl[tl.x].status, 1);
+      if (!(b < INFINITY)) atomicOr(&ctl[tl.x].status, 1);
     }
     __syncthreads();
   }

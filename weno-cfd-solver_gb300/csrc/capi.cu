@@ -627,7 +627,20 @@ int weno_solver_info(weno_solver* s, double* t, int64_t* steps, int* status) {
   WENO_CK(cudaStreamSynchronize(s->stream));
   if (t) *t = s->ctl_host->t;
   if (steps) *steps = s->ctl_host->steps;
-  if (status) *status = s->ctl_host->status ? WENO_ERR_NUMERIC : WENO_OK;
+  if (status) *status = s->ctl_host->status;
+  return WENO_OK;
+}
+
+int weno_solver_totals(weno_solver* s, double* out4) {
+  if (!s || !out4) return fail(WENO_ERR_ARG, "solver_totals: null argument");
+  double* d = nullptr;
+  if (!s->staging) WENO_CK(cudaMalloc(&s->staging, (size_t)(s->M * s->N * 8) * sizeof(double)));
+  d = s->staging;  // the first four doubles of the staging buffer
+  const HostView v = state_view(s, s->q);
+  if (s->prec == 32) WENO_CK((Launch<float, true>::totals(v, s->nx, s->ny, d, s->sm_count, s->stream)));
+  else WENO_CK((Launch<double, false>::totals(v, s->nx, s->ny, d, s->sm_count, s->stream)));
+  WENO_CK(cudaMemcpyAsync(out4, d, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  WENO_CK(cudaStreamSynchronize(s->stream));
   return WENO_OK;
 }
 

@@ -366,11 +366,16 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* a, double 
   atomicMax(a, (unsigned long long)__double_as_longlong(x));
 }
 
+// np.max propagates NaN (and inf dominates), so a non-finite wave speed makes
+// the maximum non-finite and dt follows, as in the driver; NaN's bit pattern
+// orders above +inf under the unsigned atomicMax.
+__device__ __forceinline__ double nan_max(double a, double b) { return (a != a || b != b) ? __longlong_as_double(0x7ff8000000000000ll) : fmax(a, b); }
+
 template <class T, bool AOS>
 __global__ void __launch_bounds__(256) k_cfl_max(CView<T> q, int64_t nx, int64_t ny, T gamma, StepCtl* ctl) {
   if (!ctl->active || ctl->cmax_preset) return;
   double best = 0.0;
-  bool bad = false;
+  bool nonpos = false;  // FP64 positivity check of the recovered density and pressure
   const int64_t total = nx * ny;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e / ny + 3, j = e % ny + 3;
@@ -384,32 +389,43 @@ __global__ void __launch_bounds__(256) k_cfl_max(CView<T> q, int64_t nx, int64_t
       const double rho = fmax(r0, kEps);
       uu = (double)q.at(i, j, 1) / rho;
       vv = (double)q.at(i, j, 2) / rho;
-      pp = fmax(((double)gamma - 1.0) * ((double)q.at(i, j, 3) - 0.5 * rho * (uu * uu + vv * vv)), kEps);
+      const double praw = ((double)gamma - 1.0) * ((double)q.at(i, j, 3) - 0.5 * rho * (uu * uu + vv * vv));
+      pp = fmax(praw, kEps);
+      if (!(r0 > 0.0) || !(praw > 0.0)) nonpos = true;
     }
     const double speed = sqrt(uu * uu + vv * vv);
     const double c = sqrt((double)gamma * pp / fmax(r0, 1e-14));
-    const double x = c + speed;
-    if (!(x >= 0.0) || isinf(x)) bad = true;
-    else best = fmax(best, x);
+    best = nan_max(best, c + speed);
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    best = fmax(best, __shfl_xor_sync(0xffffffffu, best, off));
-    bad = __any_sync(0xffffffffu, bad);
-  }
+  nonpos = __any_sync(0xffffffffu, nonpos);
+  if (nonpos && (threadIdx.x & 31) == 0) atomicOr(&ctl->status, 2);
+  for (int off = 16; off > 0; off >>= 1) best = nan_max(best, __shfl_xor_sync(0xffffffffu, best, off));
   __shared__ double sm[8];
-  __shared__ int sbad;
-  if (threadIdx.x == 0) sbad = 0;
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) {
-    sm[threadIdx.x >> 5] = best;
-    if (bad) sbad = 1;
-  }
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = best;
   __syncthreads();
   if (threadIdx.x == 0) {
     double b = sm[0];
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) b = fmax(b, sm[w]);
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) b = nan_max(b, sm[w]);
     atomic_max_nonneg(&ctl->cmax_bits, b);
-    if (sbad) atomicOr(&ctl->status, 1);
+    if (!(b < INFINITY)) atomicOr(&ctl->status, 1);
+  }
+}
+
+// FP64 sums of the four conserved planes over the interior (conservation
+// diagnostics); one block-partial per block, added with atomicAdd.
+template <class T>
+__global__ void __launch_bounds__(256) k_totals(CView<T> q, int64_t nx, int64_t ny, double* out4) {
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const int64_t total = nx * ny;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / ny + 3, j = e % ny + 3;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[k] += (double)q.at(i, j, k);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out4 + k, acc[k]);
   }
 }
 

@@ -59,6 +59,7 @@ struct Launch {
   static cudaError_t cfl_max(HostView q, bool aos, int64_t nx, int64_t ny, double gamma, StepCtl* ctl,
                              int sm_count, cudaStream_t st);
   static cudaError_t export_aos8(HostPlanes Q, int64_t M, int64_t N, double gamma, double* out, cudaStream_t st);
+  static cudaError_t totals(HostView q, int64_t nx, int64_t ny, double* out4, int sm_count, cudaStream_t st);
   static cudaError_t import_planes(HostView q, int64_t M, int64_t N, HostPlanes Q, cudaStream_t st);
 };
 

@@ -195,6 +195,17 @@ cudaError_t Launch<T, FAST>::export_aos8(HostPlanes Q, int64_t M, int64_t N, dou
 }
 
 template <class T, bool FAST>
+cudaError_t Launch<T, FAST>::totals(HostView q, int64_t nx, int64_t ny, double* out4, int sm_count, cudaStream_t st) {
+  int64_t blocks = (nx * ny + 255) / 256;
+  if (blocks > (int64_t)sm_count * 4) blocks = (int64_t)sm_count * 4;
+  if (blocks < 1) blocks = 1;
+  cudaError_t e = cudaMemsetAsync(out4, 0, 4 * sizeof(double), st);
+  if (e) return e;
+  k_totals<T><<<(unsigned)blocks, 256, 0, st>>>(detail::cview<T>(q), nx, ny, out4);
+  return cudaGetLastError();
+}
+
+template <class T, bool FAST>
 cudaError_t Launch<T, FAST>::import_planes(HostView q, int64_t M, int64_t N, HostPlanes Q, cudaStream_t st) {
   using namespace detail;
   const dim3 g = grid2d(M, N, kBlk);

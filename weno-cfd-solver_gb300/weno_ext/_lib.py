@@ -41,6 +41,7 @@ SIGNATURES = {
     "weno_solver_get_state": (_i, [_vp, _vp]),
     "weno_solver_get_state_host": (_i, [_vp, _vp]),
     "weno_solver_info": (_i, [_vp, ctypes.POINTER(_d), ctypes.POINTER(_i64), ctypes.POINTER(_i)]),
+    "weno_solver_totals": (_i, [_vp, ctypes.POINTER(_d)]),
     "weno_solver_enable_timing": (_i, [_vp, _i]),
     "weno_solver_timing_report": (_i, [_vp, ctypes.POINTER(_d), ctypes.POINTER(_i64), _i]),
     "weno_solver_launches_per_step": (_i, [_vp]),
@@ -48,7 +49,7 @@ SIGNATURES = {
     "weno_batch_tile_config_count": (_i, []),
     "weno_batch_create": (_i, [ctypes.POINTER(_vp), _i64, _i, _i, _i, _i, _i, _d, _d, _d, _d, _i, _vp]),
     "weno_batch_destroy": (_i, [_vp]),
-    "weno_batch_add": (_i, [_vp, _i64, _i64, _d, _i, _i64, _vp, _d, _i64, _vp, _i64, _i64, _i64, _i64,
+    "weno_batch_add": (_i, [_vp, _i64, _i64, _d, _i, _i64, _vp, _d, _i64, _d, _vp, _i64, _i64, _i64, _i64,
                             ctypes.POINTER(_i)]),
     "weno_batch_remove": (_i, [_vp, _i]),
     "weno_batch_run": (_i, [_vp, _i64, _i]),

@@ -43,7 +43,7 @@ class Batch:
     def tile_configs():
         return _lib.load().weno_batch_tile_config_count()
 
-    def add(self, q, dx, *, t_end=None, max_steps=None, bc="transmissive", bound=0, post=None):
+    def add(self, q, dx, *, t_end=None, max_steps=None, bc="transmissive", bound=0, post=None, cfl=None):
         """Add a solve from its (nx+6, ny+6, C>=4) array (numpy or torch CUDA); returns its slot."""
         torch = self._torch
         if not isinstance(q, torch.Tensor):
@@ -59,7 +59,8 @@ class Batch:
         _lib.check(self.L.weno_batch_add(
             self._h, M - 6, N - 6, float(dx), {"transmissive": _lib.BC_TRANSMISSIVE, "dmr": _lib.BC_DMR}[bc],
             int(bound), post8.ctypes.data, -1.0 if t_end is None else float(t_end),
-            0 if max_steps is None else int(max_steps), q.data_ptr(), C, s[0], s[1], s[2], ctypes.byref(slot)),
+            0 if max_steps is None else int(max_steps), -1.0 if cfl is None else float(cfl), q.data_ptr(), C, s[0],
+            s[1], s[2], ctypes.byref(slot)),
             "batch add")
         self.shapes[slot.value] = (M - 6, N - 6)
         return slot.value

@@ -94,6 +94,12 @@ class Solver:
         _lib.check(self.L.weno_solver_info(self._h, ctypes.byref(t), ctypes.byref(n), ctypes.byref(st)), "info")
         return t.value, n.value, st.value
 
+    def totals(self):
+        """FP64 sums of rho, rho*u, rho*v, E over the interior cells."""
+        out = (ctypes.c_double * 4)()
+        _lib.check(self.L.weno_solver_totals(self._h, out), "totals")
+        return tuple(out)
+
     @property
     def t(self):
         return self.info()[0]
