@@ -128,9 +128,11 @@ enum { WENO_BC_TRANSMISSIVE = 0, WENO_BC_DMR = 1 };
 
 typedef struct weno_solver weno_solver;
 
+/* weno_eps: the WENO5 smoothness epsilon (<= 0: the reference's 1e-12,
+ * weno.rs:223 / utils.rs:3); the density and pressure floors stay 1e-12. */
 int weno_solver_create(weno_solver** out, int64_t nx, int64_t ny, double dx, double gamma, int precision, int mode,
-                       int cons, int force_hlle, double jp_lo, double jp_hi, double cfl, int bc_kind, int64_t bound,
-                       const double* post8, void* stream);
+                       int cons, int force_hlle, double jp_lo, double jp_hi, double cfl, double weno_eps, int bc_kind,
+                       int64_t bound, const double* post8, void* stream);
 int weno_solver_destroy(weno_solver* s);
 /* Load the state from a device array (nx+6, ny+6, c>=4).  With c >= 8 the
  * first step's dt uses the primitive channels 5..7 as the driver does. */
@@ -177,8 +179,8 @@ typedef struct weno_batch weno_batch;
 
 int weno_batch_tile_config_count(void);
 int weno_batch_create(weno_batch** out, int64_t pool_cells, int max_solves, int precision, int mode, int cons,
-                      int force_hlle, double gamma, double jp_lo, double jp_hi, double cfl, int tile_config,
-                      void* stream);
+                      int force_hlle, double gamma, double jp_lo, double jp_hi, double cfl, double weno_eps,
+                      int tile_config, void* stream);
 int weno_batch_destroy(weno_batch* b);
 /* Add a solve from a device array (nx+6, ny+6, c>=4) (ghost cells ignored);
  * t_end < 0 for step-count only; max_steps <= 0 for no cap; cfl <= 0 takes the

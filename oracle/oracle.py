@@ -43,6 +43,8 @@ def lib():
     if _lib is None:
         build()
         L = ctypes.CDLL(_LIB_PATH)
+        L.orc_set_weno_eps.argtypes = [ctypes.c_double]
+        L.orc_set_weno_eps.restype = None
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_set_threads.restype = ctypes.c_int
         L.orc_flux.argtypes = [_c_dp, _i64, _i64, _i64, _i64, _i64, _i64, ctypes.c_double, ctypes.c_int, _c_dp]
@@ -71,6 +73,11 @@ def lib():
                                    ctypes.c_int, _i64, _c_dp]
         _lib = L
     return _lib
+
+
+def set_weno_eps(eps: float) -> None:
+    """WENO smoothness epsilon of every later call (1e-12 = the reference's DEFAULT_EPS)."""
+    lib().orc_set_weno_eps(float(eps))
 
 
 def set_threads(n: int) -> int:

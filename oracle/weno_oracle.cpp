@@ -75,6 +75,9 @@ const double DEFAULT_EPS = 1e-12;
 const double SQRT3_12 = 0.1443375673;
 const double RHO_MIN = 1e-12;
 const double P_MIN = 1e-12;
+// The WENO smoothness epsilon: DEFAULT_EPS in the reference (weno.rs:223);
+// configurable for configurations that name another value.
+static double g_weno_eps = DEFAULT_EPS;
 
 // Dense (m, n, 4) array with the layout of an ndarray Array3 in C order.
 template <class T>
@@ -255,7 +258,7 @@ static T weno5_left(T u0, T u1, T u2, T u3, T u4) {
   T beta1 = c13 * (t * t) + T(0.25) * (s * s);
   t = u0 - T(2.0) * u1 + u2; s = u0 - T(4.0) * u1 + T(3.0) * u2;
   T beta2 = c13 * (t * t) + T(0.25) * (s * s);
-  T e0 = T(DEFAULT_EPS) + beta0, e1 = T(DEFAULT_EPS) + beta1, e2 = T(DEFAULT_EPS) + beta2;
+  T e0 = T(g_weno_eps) + beta0, e1 = T(g_weno_eps) + beta1, e2 = T(g_weno_eps) + beta2;
   T a0 = T(0.3) / (e0 * e0);
   T a1 = T(0.6) / (e1 * e1);
   T a2 = T(0.1) / (e2 * e2);
@@ -278,7 +281,7 @@ static T weno5_right(T u1, T u2, T u3, T u4, T u5) {
   T beta1 = c13 * (t * t) + T(0.25) * (s * s);
   t = u1 - T(2.0) * u2 + u3; s = u1 - T(4.0) * u2 + T(3.0) * u3;
   T beta2 = c13 * (t * t) + T(0.25) * (s * s);
-  T e0 = T(DEFAULT_EPS) + beta0, e1 = T(DEFAULT_EPS) + beta1, e2 = T(DEFAULT_EPS) + beta2;
+  T e0 = T(g_weno_eps) + beta0, e1 = T(g_weno_eps) + beta1, e2 = T(g_weno_eps) + beta2;
   T a0 = T(0.1) / (e0 * e0);
   T a1 = T(0.6) / (e1 * e1);
   T a2 = T(0.3) / (e2 * e2);
@@ -305,7 +308,7 @@ static T weno5_gq(T q0, T q1, T q2, T q3, T q4, bool second) {
   T d0 = second ? T(0.1960481952) : T(0.1928406937);
   T d1 = T(0.6111111111);
   T d2 = second ? T(0.1928406937) : T(0.1960481952);
-  T e0 = T(DEFAULT_EPS) + beta0, e1 = T(DEFAULT_EPS) + beta1, e2 = T(DEFAULT_EPS) + beta2;
+  T e0 = T(g_weno_eps) + beta0, e1 = T(g_weno_eps) + beta1, e2 = T(g_weno_eps) + beta2;
   T a0 = d0 / (e0 * e0);
   T a1 = d1 / (e1 * e1);
   T a2 = d2 / (e2 * e2);
@@ -607,6 +610,8 @@ static A3<double> dense4(const double* p, int64_t m, int64_t n, int64_t c) {
 }
 
 extern "C" {
+
+void orc_set_weno_eps(double eps) { g_weno_eps = eps > 0.0 ? eps : DEFAULT_EPS; }
 
 int orc_set_threads(int n) {
 #ifdef _OPENMP

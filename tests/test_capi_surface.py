@@ -53,7 +53,7 @@ def test_library_builds_and_exports_every_declared_symbol():
     # and the ctypes binding covers exactly the declared functions
     assert sorted(_lib.SIGNATURES) == header_functions()
     L = _lib.load()
-    assert L.weno_abi_version() == 1
+    assert L.weno_abi_version() == 2
 
 
 def test_reference_api_surface():

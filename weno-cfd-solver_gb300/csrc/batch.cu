@@ -49,7 +49,7 @@ inline long long align64(long long x) { return (x + 63) / 64 * 64; }
 struct weno_batch {
   int prec = 32, mode = WENO_FAST;
   bool chr = false, blend = false;
-  double gamma = 1.4, jp_lo = 0.2, jp_hi = 1.0, cfl = 0.5;
+  double gamma = 1.4, jp_lo = 0.2, jp_hi = 1.0, cfl = 0.5, weps = 1e-12;
   int cfg = 1;
   int max_solves = 0;
   long long capacity = 0;  // elements per pool
@@ -90,7 +90,7 @@ cudaError_t enqueue_batch_step(weno_batch* b) {
     const void* qin = b->pool[s == 1 ? 0 : (s == 2 ? 1 : 2)];
     void* qo = b->pool[s == 1 ? 1 : (s == 2 ? 2 : 0)];
     if ((e = BL::stage(b->cfg, b->chr, b->blend, b->d_solves, b->d_ctl, b->d_tiles, b->ntiles, grid, qin, b->pool[0],
-                       qo, s, b->gamma, b->jp_lo, b->jp_hi, b->stream)))
+                       qo, s, b->gamma, b->jp_lo, b->jp_hi, b->weps, b->stream)))
       return e;
   }
   return BL::clock(b->d_ctl, b->max_solves, 1, b->stream);
@@ -237,8 +237,8 @@ extern "C" {
 int weno_batch_tile_config_count(void) { return kNumTileConfigs; }
 
 int weno_batch_create(weno_batch** out, int64_t pool_cells, int max_solves, int precision, int mode, int cons,
-                      int force_hlle, double gamma, double jp_lo, double jp_hi, double cfl, int tile_config,
-                      void* stream) {
+                      int force_hlle, double gamma, double jp_lo, double jp_hi, double cfl, double weno_eps,
+                      int tile_config, void* stream) {
   if (!out) return bfail(WENO_ERR_ARG, "batch_create: null handle pointer");
   *out = nullptr;
   if (pool_cells <= 0 || max_solves <= 0) return bfail(WENO_ERR_ARG, "batch_create: empty pool");
@@ -255,6 +255,7 @@ int weno_batch_create(weno_batch** out, int64_t pool_cells, int max_solves, int 
   b->jp_lo = jp_lo;
   b->jp_hi = jp_hi;
   b->cfl = cfl;
+  b->weps = weno_eps > 0.0 ? weno_eps : 1e-12;
   b->cfg = tile_config;
   b->max_solves = max_solves;
   b->es = precision == 32 ? 4 : 8;

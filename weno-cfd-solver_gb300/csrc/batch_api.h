@@ -23,7 +23,7 @@ struct BatchLaunch {
   static int ctas_per_sm(int cfg, bool chr, bool blend);
   static cudaError_t stage(int cfg, bool chr, bool blend, const SolveDesc* solves, SolveCtl* ctl, const void* tiles,
                            int ntiles, int grid, const void* qin, const void* qn, void* qo, int stage, double gamma,
-                           double jp_lo, double jp_hi, cudaStream_t st);
+                           double jp_lo, double jp_hi, double weps, cudaStream_t st);
   static cudaError_t cfl(int cfg, const SolveDesc* solves, SolveCtl* ctl, const void* tiles, int ntiles, int grid,
                          const void* q, double gamma, cudaStream_t st);
   static cudaError_t clock(SolveCtl* ctl, int nsolves, int phase, cudaStream_t st);

@@ -18,7 +18,7 @@ constexpr size_t tile_smem() {
 
 template <class T, bool FAST, bool CHAR, bool BLEND, int TX, int TY>
 cudaError_t launch_stage(const SolveDesc* solves, SolveCtl* ctl, const int4* tiles, int ntiles, int grid, const T* qin,
-                         const T* qn, T* qo, int stage, T gamma, T jp_lo, T jp_hi, cudaStream_t st) {
+                         const T* qn, T* qo, int stage, T gamma, T jp_lo, T jp_hi, T weps, cudaStream_t st) {
   constexpr size_t sm = tile_smem<T, TX, TY, BLEND>();
   if constexpr (sm > 227 * 1024) {
     return cudaErrorInvalidConfiguration;
@@ -30,7 +30,7 @@ cudaError_t launch_stage(const SolveDesc* solves, SolveCtl* ctl, const int4* til
       if (e != cudaSuccess) return e;
       attr_set = true;
     }
-    k<<<grid, kNT, sm, st>>>(solves, ctl, tiles, ntiles, qin, qn, qo, stage, gamma, jp_lo, jp_hi);
+    k<<<grid, kNT, sm, st>>>(solves, ctl, tiles, ntiles, qin, qn, qo, stage, gamma, jp_lo, jp_hi, weps);
     return cudaGetLastError();
   }
 }
@@ -87,7 +87,7 @@ template <class T, bool FAST>
 cudaError_t BatchLaunch<T, FAST>::stage(int cfg, bool chr, bool blend, const SolveDesc* solves, SolveCtl* ctl,
                                         const void* tiles, int ntiles, int grid, const void* qin, const void* qn,
                                         void* qo, int stage, double gamma, double jp_lo, double jp_hi,
-                                        cudaStream_t st) {
+                                        double weps, cudaStream_t st) {
   if (ntiles <= 0 || grid <= 0) return cudaSuccess;
   const int4* tl = static_cast<const int4*>(tiles);
   const T* a = static_cast<const T*>(qin);
@@ -97,16 +97,16 @@ cudaError_t BatchLaunch<T, FAST>::stage(int cfg, bool chr, bool blend, const Sol
 #define WENO_ST(TX, TY)                                                                                           \
   if (chr && blend)                                                                                               \
     e = bdetail::launch_stage<T, FAST, true, true, TX, TY>(solves, ctl, tl, ntiles, grid, a, b, o, stage, (T)gamma, \
-                                                           (T)jp_lo, (T)jp_hi, st);                               \
+                                                           (T)jp_lo, (T)jp_hi, (T)weps, st);                               \
   else if (chr)                                                                                                   \
     e = bdetail::launch_stage<T, FAST, true, false, TX, TY>(solves, ctl, tl, ntiles, grid, a, b, o, stage,         \
-                                                            (T)gamma, (T)jp_lo, (T)jp_hi, st);                    \
+                                                            (T)gamma, (T)jp_lo, (T)jp_hi, (T)weps, st);                    \
   else if (blend)                                                                                                 \
     e = bdetail::launch_stage<T, FAST, false, true, TX, TY>(solves, ctl, tl, ntiles, grid, a, b, o, stage,         \
-                                                            (T)gamma, (T)jp_lo, (T)jp_hi, st);                    \
+                                                            (T)gamma, (T)jp_lo, (T)jp_hi, (T)weps, st);                    \
   else                                                                                                            \
     e = bdetail::launch_stage<T, FAST, false, false, TX, TY>(solves, ctl, tl, ntiles, grid, a, b, o, stage,        \
-                                                             (T)gamma, (T)jp_lo, (T)jp_hi, st);
+                                                             (T)gamma, (T)jp_lo, (T)jp_hi, (T)weps, st);
   WENO_TILE_SWITCH(cfg, WENO_ST)
 #undef WENO_ST
   return e;

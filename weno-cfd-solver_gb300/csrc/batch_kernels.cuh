@@ -137,7 +137,8 @@ __device__ __forceinline__ T tile_sensor(const T* pbar, int R, int C, int fr, in
 template <class T, bool FAST, bool CHAR, bool BLEND, int TX, int TY, int NT>
 __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict__ solves, SolveCtl* ctl,
                                                      const int4* __restrict__ tiles, int ntiles, const T* Qin,
-                                                     const T* Qn, T* Qo, int stage, T gamma, T jp_lo, T jp_hi) {
+                                                     const T* Qn, T* Qo, int stage, T gamma, T jp_lo, T jp_hi,
+                                                     T weps) {
   using G = TileGeom<TX, TY, BLEND>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* U = reinterpret_cast<T*>(smem_raw);
@@ -191,7 +192,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
 #pragma unroll
         for (int k = 0; k < 4; ++k) cells[s][k] = U[k * G::UR * G::UC + (fr + s) * G::UC + c + 1];
       T ql[4], qr[4];
-      pass1_face<T, FAST, false, CHAR>(cells, gamma, ql, qr);
+      pass1_face<T, FAST, false, CHAR>(cells, gamma, ql, qr, weps);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         P1[k * G::P1 + e] = ql[k];
@@ -210,7 +211,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const T* p = P1 + k * G::P1 + fr * G::P1XC + fc;
-          weno5_gq_pair<T, FAST>(p[0], p[1], p[2], p[3], p[4], a1[k], a2[k]);
+          weno5_gq_pair<T, FAST>(p[0], p[1], p[2], p[3], p[4], a1[k], a2[k], weps);
         }
         euler_flux<T, FAST, false>(a1, gamma, f1);
         euler_flux<T, FAST, false>(a2, gamma, f2);
@@ -222,7 +223,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const T* p = P1 + (4 + k) * G::P1 + fr * G::P1XC + fc;
-          weno5_gq_pair<T, FAST>(p[0], p[1], p[2], p[3], p[4], a1[k], a2[k]);
+          weno5_gq_pair<T, FAST>(p[0], p[1], p[2], p[3], p[4], a1[k], a2[k], weps);
         }
         euler_flux<T, FAST, false>(a1, gamma, f1);
         euler_flux<T, FAST, false>(a2, gamma, f2);
@@ -263,7 +264,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
 #pragma unroll
         for (int k = 0; k < 4; ++k) cells[s][k] = U[k * G::UR * G::UC + (r + 1) * G::UC + fc + s];
       T ql[4], qr[4];
-      pass1_face<T, FAST, true, CHAR>(cells, gamma, ql, qr);
+      pass1_face<T, FAST, true, CHAR>(cells, gamma, ql, qr, weps);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         P1[k * G::P1 + e] = ql[k];
@@ -282,7 +283,8 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const T* p = P1 + k * G::P1 + fr * G::P1YC + fc;
-          weno5_gq_pair<T, FAST>(p[0], p[G::P1YC], p[2 * G::P1YC], p[3 * G::P1YC], p[4 * G::P1YC], a1[k], a2[k]);
+          weno5_gq_pair<T, FAST>(p[0], p[G::P1YC], p[2 * G::P1YC], p[3 * G::P1YC], p[4 * G::P1YC], a1[k], a2[k],
+                                 weps);
         }
         euler_flux<T, FAST, true>(a1, gamma, f1);
         euler_flux<T, FAST, true>(a2, gamma, f2);
@@ -294,7 +296,8 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const T* p = P1 + (4 + k) * G::P1 + fr * G::P1YC + fc;
-          weno5_gq_pair<T, FAST>(p[0], p[G::P1YC], p[2 * G::P1YC], p[3 * G::P1YC], p[4 * G::P1YC], a1[k], a2[k]);
+          weno5_gq_pair<T, FAST>(p[0], p[G::P1YC], p[2 * G::P1YC], p[3 * G::P1YC], p[4 * G::P1YC], a1[k], a2[k],
+                                 weps);
         }
         euler_flux<T, FAST, true>(a1, gamma, f1);
         euler_flux<T, FAST, true>(a2, gamma, f2);

@@ -81,7 +81,7 @@ template <class T, bool FAST>
 cudaError_t residual_pipeline(HostView u, int64_t m, int64_t n, const ResidualLayout& Lo, void* ws, double gamma,
                               double dx, bool force_hlle, double jp_lo, double jp_hi, bool cons, int stage, void* out,
                               HostPlanes Qn, HostPlanes Qs, HostPlanes Qo, const StepCtl* ctl, cudaStream_t st,
-                              TimingHook tm = TimingHook()) {
+                              TimingHook tm = TimingHook(), double weps = 1e-12) {
   using Lx = Launch<T, FAST>;
   const int kind = force_hlle ? 1 : 2;
   T* fx = static_cast<T*>(at(ws, Lo.off_fx));
@@ -95,9 +95,9 @@ cudaError_t residual_pipeline(HostView u, int64_t m, int64_t n, const ResidualLa
     if ((e = (call)) != cudaSuccess) return e;             \
     if ((e = tm(cls, false)) != cudaSuccess) return e;     \
   } while (0)
-  WENO_TIMED(HC_PASS1_X, Lx::pass1(u, m - 5, n, gamma, false, !cons, PL, PR, st));
+  WENO_TIMED(HC_PASS1_X, Lx::pass1(u, m - 5, n, gamma, false, !cons, PL, PR, weps, st));
   WENO_TIMED(HC_PASS2_X, Lx::pass2(PL, PR, m - 5, n - 6, gamma, false, kind, fx, fx + 4 * Lo.FX, fx + 8 * Lo.FX,
-                                   nullptr, Lo.FX, n - 6, st));
+                                   nullptr, Lo.FX, n - 6, weps, st));
   if (!force_hlle) {
     HostPlanes C{fx, Lo.FX, n - 6}, E{fx + 4 * Lo.FX, Lo.FX, n - 6}, P{fx + 8 * Lo.FX, Lo.FX, n - 6};
     WENO_TIMED(HC_BLEND, Lx::blend(C, E, P, m - 5, n - 6, jp_lo, jp_hi, nullptr, st));
@@ -105,9 +105,9 @@ cudaError_t residual_pipeline(HostView u, int64_t m, int64_t n, const ResidualLa
   // y sweep
   PL.ld = n - 5;
   PR.ld = n - 5;
-  WENO_TIMED(HC_PASS1_Y, Lx::pass1(u, m, n - 5, gamma, true, !cons, PL, PR, st));
+  WENO_TIMED(HC_PASS1_Y, Lx::pass1(u, m, n - 5, gamma, true, !cons, PL, PR, weps, st));
   WENO_TIMED(HC_PASS2_Y, Lx::pass2(PL, PR, m - 6, n - 5, gamma, true, kind, fy, fy + 4 * Lo.FY, fy + 8 * Lo.FY,
-                                   nullptr, Lo.FY, n - 5, st));
+                                   nullptr, Lo.FY, n - 5, weps, st));
   if (!force_hlle) {
     HostPlanes C{fy, Lo.FY, n - 5}, E{fy + 4 * Lo.FY, Lo.FY, n - 5}, P{fy + 8 * Lo.FY, Lo.FY, n - 5};
     WENO_TIMED(HC_BLEND, Lx::blend(C, E, P, m - 6, n - 5, jp_lo, jp_hi, nullptr, st));
@@ -154,7 +154,7 @@ extern "C" {
 
 const char* weno_last_error(void) { return g_err.c_str(); }
 
-int weno_abi_version(void) { return 1; }
+int weno_abi_version(void) { return 2; }
 
 int weno_flux(const double* q, int64_t m, int64_t n, int64_t c, int64_t s0, int64_t s1, int64_t s2, double gamma,
               int ydir, int mode, double* out, void* stream) {
@@ -202,11 +202,12 @@ int weno_reconstruct(const double* u, int64_t m, int64_t n, int64_t c, int64_t s
   HostView v{u, s0, s1, s2};
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (mode == WENO_FAST) {
-    WENO_CK((Launch<double, true>::pass1(v, r1, c1, gamma, ydir != 0, cons == 0, PL, PR, st)));
-    WENO_CK((Launch<double, true>::pass2(PL, PR, r2, c2, gamma, ydir != 0, 0, q_l, f_l, q_r, f_r, 0, 0, st)));
+    WENO_CK((Launch<double, true>::pass1(v, r1, c1, gamma, ydir != 0, cons == 0, PL, PR, 1e-12, st)));
+    WENO_CK((Launch<double, true>::pass2(PL, PR, r2, c2, gamma, ydir != 0, 0, q_l, f_l, q_r, f_r, 0, 0, 1e-12, st)));
   } else {
-    WENO_CK((Launch<double, false>::pass1(v, r1, c1, gamma, ydir != 0, cons == 0, PL, PR, st)));
-    WENO_CK((Launch<double, false>::pass2(PL, PR, r2, c2, gamma, ydir != 0, 0, q_l, f_l, q_r, f_r, 0, 0, st)));
+    WENO_CK((Launch<double, false>::pass1(v, r1, c1, gamma, ydir != 0, cons == 0, PL, PR, 1e-12, st)));
+    WENO_CK((Launch<double, false>::pass2(PL, PR, r2, c2, gamma, ydir != 0, 0, q_l, f_l, q_r, f_r, 0, 0, 1e-12,
+                                          st)));
   }
   return WENO_OK;
 }
@@ -343,7 +344,7 @@ struct weno_solver {
   cudaStream_t stream = nullptr;
   int prec = 64, mode = WENO_EXACT;
   bool cons = false, force_hlle = true;
-  double jp_lo = 0, jp_hi = 0, cfl = 0.5, dx = 1, gamma = 1.4;
+  double jp_lo = 0, jp_hi = 0, cfl = 0.5, dx = 1, gamma = 1.4, weps = 1e-12;
   int bc_kind = WENO_BC_TRANSMISSIVE;
   int64_t bound = 0;
   double post8[8] = {0};
@@ -427,7 +428,7 @@ cudaError_t enqueue_step_t(weno_solver* s, int* launches) {
   for (int k = 0; k < 3; ++k) {
     if ((e = residual_pipeline<T, FAST>(state_view(s, stages[k].in), s->M, s->N, *s->layout, s->ws, s->gamma, s->dx,
                                         s->force_hlle, s->jp_lo, s->jp_hi, s->cons, k + 1, nullptr, Q, stages[k].qs,
-                                        stages[k].qo, s->ctl, st, tm)))
+                                        stages[k].qo, s->ctl, st, tm, s->weps)))
       return e;
     if ((e = tm(TC_BC, true))) return e;
     if ((e = bc_state<T, FAST>(s, stages[k].qo.p))) return e;
@@ -467,8 +468,8 @@ void solver_free(weno_solver* s) {
 extern "C" {
 
 int weno_solver_create(weno_solver** out, int64_t nx, int64_t ny, double dx, double gamma, int precision, int mode,
-                       int cons, int force_hlle, double jp_lo, double jp_hi, double cfl, int bc_kind, int64_t bound,
-                       const double* post8, void* stream) {
+                       int cons, int force_hlle, double jp_lo, double jp_hi, double cfl, double weno_eps, int bc_kind,
+                       int64_t bound, const double* post8, void* stream) {
   if (!out) return fail(WENO_ERR_ARG, "solver_create: null handle pointer");
   *out = nullptr;
   if (nx < 3 || ny < 3) return fail(WENO_ERR_SHAPE, "solver_create: nx, ny >= 3 required, got (%lld, %lld)",
@@ -488,6 +489,7 @@ int weno_solver_create(weno_solver** out, int64_t nx, int64_t ny, double dx, dou
   s->jp_lo = jp_lo;
   s->jp_hi = jp_hi;
   s->cfl = cfl;
+  s->weps = weno_eps > 0.0 ? weno_eps : 1e-12;
   s->dx = dx;
   s->gamma = gamma;
   s->bc_kind = bc_kind;

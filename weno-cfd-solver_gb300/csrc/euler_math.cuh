@@ -28,7 +28,8 @@ namespace weno {
 inline namespace WENO_TU_NS {
 
 // utils.rs:3-6
-constexpr double kEps = 1e-12;              // DEFAULT_EPS, RHO_MIN and P_MIN
+constexpr double kEps = 1e-12;              // DEFAULT_EPS, RHO_MIN and P_MIN; also the default WENO epsilon
+                                            // `weps` (weno.rs:223), which callers may change
 constexpr double kSqrt3_12 = 0.1443375673;  // truncated literal, not sqrt(3)/12
 // weno.rs:270 / weno.rs:292 (Gauss-point linear weights, 10 digits)
 constexpr double kGqA0 = 0.1928406937, kGqA1 = 0.6111111111, kGqA2 = 0.1960481952;
@@ -188,18 +189,18 @@ __device__ __forceinline__ T weno_combine(T e0, T e1, T e2, T d0, T d1, T d2, T 
 
 // weno.rs:214-233 (left-biased, value at the right face of u2)
 template <class T, bool FAST>
-__device__ __forceinline__ T weno5_left(T u0, T u1, T u2, T u3, T u4) {
+__device__ __forceinline__ T weno5_left(T u0, T u1, T u2, T u3, T u4, T weps) {
   T b0, b1, b2;
   js_betas(u0, u1, u2, u3, u4, b0, b1, b2);
   const T p0 = -u4 + T(5.0) * u3 + T(2.0) * u2;
   const T p1 = -u1 + T(5.0) * u2 + T(2.0) * u3;
   const T p2 = T(2.0) * u0 - T(7.0) * u1 + T(11.0) * u2;
-  return weno_combine<T, FAST>(T(kEps) + b0, T(kEps) + b1, T(kEps) + b2, T(0.3), T(0.6), T(0.1), p0, p1, p2, T(6.0));
+  return weno_combine<T, FAST>(weps + b0, weps + b1, weps + b2, T(0.3), T(0.6), T(0.1), p0, p1, p2, T(6.0));
 }
 
 // weno.rs:238-257 (right-biased, value at the left face of u3)
 template <class T, bool FAST>
-__device__ __forceinline__ T weno5_right(T u1, T u2, T u3, T u4, T u5) {
+__device__ __forceinline__ T weno5_right(T u1, T u2, T u3, T u4, T u5, T weps) {
   T b0, b1, b2;
   T t, s;
   t = u3 - T(2.0) * u4 + u5;
@@ -214,16 +215,16 @@ __device__ __forceinline__ T weno5_right(T u1, T u2, T u3, T u4, T u5) {
   const T p0 = T(2.0) * u5 - T(7.0) * u4 + T(11.0) * u3;
   const T p1 = -u4 + T(5.0) * u3 + T(2.0) * u2;
   const T p2 = -u1 + T(5.0) * u2 + T(2.0) * u3;
-  return weno_combine<T, FAST>(T(kEps) + b0, T(kEps) + b1, T(kEps) + b2, T(0.1), T(0.6), T(0.3), p0, p1, p2, T(6.0));
+  return weno_combine<T, FAST>(weps + b0, weps + b1, weps + b2, T(0.1), T(0.6), T(0.3), p0, p1, p2, T(6.0));
 }
 
 // weno.rs:262-303: both Gauss-point values from one 5-cell stencil.  The
 // smoothness indicators are shared (the reference recomputes identical values).
 template <class T, bool FAST>
-__device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& ra, T& rb) {
+__device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& ra, T& rb, T weps) {
   T b0, b1, b2;
   js_betas(q0, q1, q2, q3, q4, b0, b1, b2);
-  const T e0 = T(kEps) + b0, e1 = T(kEps) + b1, e2 = T(kEps) + b2;
+  const T e0 = weps + b0, e1 = weps + b1, e2 = weps + b2;
   const T S = T(kSqrt3_12);
   const T g0 = T(3.0) * q2 - T(4.0) * q3 + q4;
   const T g2 = T(3.0) * q2 - T(4.0) * q1 + q0;
@@ -415,12 +416,12 @@ __device__ __forceinline__ void pp_limit(T q[4], const T ub[4], T gamma) {
 // weno.rs:654-717 component-wise).  c[0..5] are the six cells along the normal.
 // ---------------------------------------------------------------------------
 template <class T, bool FAST, bool Y, bool CHAR>
-__device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T qr[4]) {
+__device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T qr[4], T weps) {
   if constexpr (!CHAR) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      ql[k] = weno5_left<T, FAST>(c[0][k], c[1][k], c[2][k], c[3][k], c[4][k]);
-      qr[k] = weno5_right<T, FAST>(c[1][k], c[2][k], c[3][k], c[4][k], c[5][k]);
+      ql[k] = weno5_left<T, FAST>(c[0][k], c[1][k], c[2][k], c[3][k], c[4][k], weps);
+      qr[k] = weno5_right<T, FAST>(c[1][k], c[2][k], c[3][k], c[4][k], c[5][k], weps);
     }
   } else {
     T rho_a, u_a, v_a, h_a, c_a;
@@ -436,8 +437,8 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
     T chl[4], chr[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      chl[k] = weno5_left<T, FAST>(w[0][k], w[1][k], w[2][k], w[3][k], w[4][k]);
-      chr[k] = weno5_right<T, FAST>(w[1][k], w[2][k], w[3][k], w[4][k], w[5][k]);
+      chl[k] = weno5_left<T, FAST>(w[0][k], w[1][k], w[2][k], w[3][k], w[4][k], weps);
+      chr[k] = weno5_right<T, FAST>(w[1][k], w[2][k], w[3][k], w[4][k], w[5][k], weps);
     }
     T Rm[4][4];
     right_eig<T, Y>(rho_a, u_a, v_a, h_a, c_a, Rm);

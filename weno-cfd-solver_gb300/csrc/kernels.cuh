@@ -43,7 +43,7 @@ struct Planes {
 // ---------------------------------------------------------------------------
 template <class T, bool FAST, bool Y, bool CHAR>
 __global__ void __launch_bounds__(128) k_pass1(CView<T> u, int64_t rows, int64_t cols, T gamma, Planes<T> PL,
-                                                Planes<T> PR) {
+                                                Planes<T> PR, T weps) {
   const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t row = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
   if (row >= rows || col >= cols) return;
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(128) k_pass1(CView<T> u, int64_t rows, int64_t
 #pragma unroll
     for (int k = 0; k < 4; ++k) c[s][k] = Y ? u.at(row, col + s, k) : u.at(row + s, col, k);
   T ql[4], qr[4];
-  pass1_face<T, FAST, Y, CHAR>(c, gamma, ql, qr);
+  pass1_face<T, FAST, Y, CHAR>(c, gamma, ql, qr, weps);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     PL.at(k, row, col) = ql[k];
@@ -79,26 +79,26 @@ struct Pass2Dst {
 };
 
 template <class T, bool FAST, bool Y>
-__device__ __forceinline__ void gq_face(const Planes<T>& P, int64_t row, int64_t col, T q1[4], T q2[4]) {
+__device__ __forceinline__ void gq_face(const Planes<T>& P, int64_t row, int64_t col, T q1[4], T q2[4], T weps) {
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     T s[5];
 #pragma unroll
     for (int t = 0; t < 5; ++t) s[t] = Y ? P.at(k, row + 1 + t, col) : P.at(k, row, col + 1 + t);
-    weno5_gq_pair<T, FAST>(s[0], s[1], s[2], s[3], s[4], q1[k], q2[k]);
+    weno5_gq_pair<T, FAST>(s[0], s[1], s[2], s[3], s[4], q1[k], q2[k], weps);
   }
 }
 
 template <class T, bool FAST, bool Y, int OUT>
 __global__ void __launch_bounds__(128) k_pass2(Planes<T> PL, Planes<T> PR, int64_t rows, int64_t cols, T gamma,
-                                                Pass2Dst dst) {
+                                                Pass2Dst dst, T weps) {
   const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t row = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
   if (row >= rows || col >= cols) return;
   T ql[4], qr[4], fl[4], fr[4];
   {
     T a1[4], a2[4], f1[4], f2[4];
-    gq_face<T, FAST, Y>(PL, row, col, a1, a2);
+    gq_face<T, FAST, Y>(PL, row, col, a1, a2, weps);
     euler_flux<T, FAST, Y>(a1, gamma, f1);
     euler_flux<T, FAST, Y>(a2, gamma, f2);
 #pragma unroll
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(128) k_pass2(Planes<T> PL, Planes<T> PR, int64
       fl[k] = T(0.5) * (f1[k] + f2[k]);
       ql[k] = T(0.5) * (a1[k] + a2[k]);
     }
-    gq_face<T, FAST, Y>(PR, row, col, a1, a2);
+    gq_face<T, FAST, Y>(PR, row, col, a1, a2, weps);
     euler_flux<T, FAST, Y>(a1, gamma, f1);
     euler_flux<T, FAST, Y>(a2, gamma, f2);
 #pragma unroll

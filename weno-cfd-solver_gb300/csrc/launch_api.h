@@ -29,12 +29,13 @@ template <class T, bool FAST>
 struct Launch {
   // Pass 1 over `rows x cols` faces (x: rows = m-5, cols = n; y: rows = m, cols = n-5).
   static cudaError_t pass1(HostView u, int64_t rows, int64_t cols, double gamma, bool ydir, bool chr,
-                           HostPlanes PL, HostPlanes PR, cudaStream_t st);
+                           HostPlanes PL, HostPlanes PR, double weps, cudaStream_t st);
   // Pass 2 over the final face array.  kind 0: dense q_l, f_l, q_r, f_r into
   // a..d; kind 1: HLLE flux planes into a; kind 2: HLLC planes into a, HLLE
   // planes into b, mean pressure plane into c.  ps/ld describe a, b, c.
   static cudaError_t pass2(HostPlanes PL, HostPlanes PR, int64_t rows, int64_t cols, double gamma, bool ydir,
-                           int kind, void* a, void* b, void* c, void* d, int64_t ps, int64_t ld, cudaStream_t st);
+                           int kind, void* a, void* b, void* c, void* d, int64_t ps, int64_t ld, double weps,
+                           cudaStream_t st);
   // Riemann solver on dense (rows, cols, 4) face arrays.  kind 0 HLLC / 1 HLLE
   // -> dense out; kind 2 -> planes Fc (a), Fe (b), pbar (c).
   static cudaError_t riemann(const void* ql, const void* fl, const void* qr, const void* fr, int64_t rows,

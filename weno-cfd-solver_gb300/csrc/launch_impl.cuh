@@ -34,22 +34,22 @@ const dim3 kBlk(32, 4, 1);
 
 template <class T, bool FAST>
 cudaError_t Launch<T, FAST>::pass1(HostView u, int64_t rows, int64_t cols, double gamma, bool ydir, bool chr,
-                                   HostPlanes PL, HostPlanes PR, cudaStream_t st) {
+                                   HostPlanes PL, HostPlanes PR, double weps, cudaStream_t st) {
   using namespace detail;
   if (rows <= 0 || cols <= 0) return cudaSuccess;
   const dim3 g = grid2d(rows, cols, kBlk);
   auto U = cview<T>(u);
   auto L = planes<T>(PL), R = planes<T>(PR);
-  if (!ydir && chr) k_pass1<T, FAST, false, true><<<g, kBlk, 0, st>>>(U, rows, cols, (T)gamma, L, R);
-  else if (!ydir) k_pass1<T, FAST, false, false><<<g, kBlk, 0, st>>>(U, rows, cols, (T)gamma, L, R);
-  else if (chr) k_pass1<T, FAST, true, true><<<g, kBlk, 0, st>>>(U, rows, cols, (T)gamma, L, R);
-  else k_pass1<T, FAST, true, false><<<g, kBlk, 0, st>>>(U, rows, cols, (T)gamma, L, R);
+  if (!ydir && chr) k_pass1<T, FAST, false, true><<<g, kBlk, 0, st>>>(U, rows, cols, (T)gamma, L, R, (T)weps);
+  else if (!ydir) k_pass1<T, FAST, false, false><<<g, kBlk, 0, st>>>(U, rows, cols, (T)gamma, L, R, (T)weps);
+  else if (chr) k_pass1<T, FAST, true, true><<<g, kBlk, 0, st>>>(U, rows, cols, (T)gamma, L, R, (T)weps);
+  else k_pass1<T, FAST, true, false><<<g, kBlk, 0, st>>>(U, rows, cols, (T)gamma, L, R, (T)weps);
   return cudaGetLastError();
 }
 
 template <class T, bool FAST>
 cudaError_t Launch<T, FAST>::pass2(HostPlanes PL, HostPlanes PR, int64_t rows, int64_t cols, double gamma, bool ydir,
-                                   int kind, void* a, void* b, void* c, void* d, int64_t ps, int64_t ld,
+                                   int kind, void* a, void* b, void* c, void* d, int64_t ps, int64_t ld, double weps,
                                    cudaStream_t st) {
   using namespace detail;
   if (rows <= 0 || cols <= 0) return cudaSuccess;
@@ -57,7 +57,7 @@ cudaError_t Launch<T, FAST>::pass2(HostPlanes PL, HostPlanes PR, int64_t rows, i
   auto L = planes<T>(PL), R = planes<T>(PR);
   Pass2Dst dst{a, b, c, d, ps, ld};
   const T gm = (T)gamma;
-#define WENO_P2(Y, K) k_pass2<T, FAST, Y, K><<<g, kBlk, 0, st>>>(L, R, rows, cols, gm, dst)
+#define WENO_P2(Y, K) k_pass2<T, FAST, Y, K><<<g, kBlk, 0, st>>>(L, R, rows, cols, gm, dst, (T)weps)
   if (!ydir) {
     if (kind == 0) WENO_P2(false, P2_STATES);
     else if (kind == 1) WENO_P2(false, P2_HLLE);

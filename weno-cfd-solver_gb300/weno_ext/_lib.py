@@ -32,8 +32,8 @@ SIGNATURES = {
     "weno_l_local": (_i, [_vp, _i64, _i64, _i64, _i64, _i64, _i64, _d, _d, _i, _d, _d, _i, _i, _vp, _vp, _sz, _vp]),
     "weno_l_local_host": (_i, [_vp, _i64, _i64, _i64, _d, _d, _i, _d, _d, _i, _i, _vp]),
     "weno_l_local_noalloc": (_i, [_vp, _i64, _i64, _i64, _i64, _i64, _i64, _d, _d, _i, _d, _d, _i, _i, _vp, _vp]),
-    "weno_solver_create": (_i, [ctypes.POINTER(_vp), _i64, _i64, _d, _d, _i, _i, _i, _i, _d, _d, _d, _i, _i64, _vp,
-                                _vp]),
+    "weno_solver_create": (_i, [ctypes.POINTER(_vp), _i64, _i64, _d, _d, _i, _i, _i, _i, _d, _d, _d, _d, _i, _i64,
+                                _vp, _vp]),
     "weno_solver_destroy": (_i, [_vp]),
     "weno_solver_set_state": (_i, [_vp, _vp, _i64, _i64, _i64, _i64]),
     "weno_solver_set_state_host": (_i, [_vp, _vp, _i64]),
@@ -47,7 +47,7 @@ SIGNATURES = {
     "weno_solver_launches_per_step": (_i, [_vp]),
     "weno_probe_rates": (_i, [ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d), _vp]),
     "weno_batch_tile_config_count": (_i, []),
-    "weno_batch_create": (_i, [ctypes.POINTER(_vp), _i64, _i, _i, _i, _i, _i, _d, _d, _d, _d, _i, _vp]),
+    "weno_batch_create": (_i, [ctypes.POINTER(_vp), _i64, _i, _i, _i, _i, _i, _d, _d, _d, _d, _d, _i, _vp]),
     "weno_batch_destroy": (_i, [_vp]),
     "weno_batch_add": (_i, [_vp, _i64, _i64, _d, _i, _i64, _vp, _d, _i64, _d, _vp, _i64, _i64, _i64, _i64,
                             ctypes.POINTER(_i)]),

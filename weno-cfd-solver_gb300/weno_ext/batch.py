@@ -21,7 +21,7 @@ from .solver import DMR_POST
 
 class Batch:
     def __init__(self, pool_cells, max_solves, *, precision=32, mode="fast", cons=True, force_hlle=False,
-                 jp_cri=(1e4, 1.1e4), gamma=1.4, cfl=0.5, tile_config=1, stream=None):
+                 jp_cri=(1e4, 1.1e4), gamma=1.4, cfl=0.5, tile_config=1, stream=None, weno_eps=1e-12):
         import torch
         if not torch.cuda.is_available():
             raise RuntimeError("Batch needs a CUDA GPU; there is no CPU fallback")
@@ -35,7 +35,8 @@ class Batch:
         _lib.check(self.L.weno_batch_create(
             ctypes.byref(h), int(pool_cells), self.max_solves, self.precision,
             _lib.FAST if mode == "fast" else _lib.EXACT, int(bool(cons)), int(bool(force_hlle)), self.gamma,
-            float(jp_cri[0]), float(jp_cri[1]), float(cfl), int(tile_config), self.stream.cuda_stream), "Batch")
+            float(jp_cri[0]), float(jp_cri[1]), float(cfl), float(weno_eps), int(tile_config), self.stream.cuda_stream),
+            "Batch")
         self._h = h
         self.shapes = {}
 

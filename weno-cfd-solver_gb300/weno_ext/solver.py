@@ -25,7 +25,7 @@ DMR_POST = (8.0, 33.0, -57.1576, 563.499, 8.0, 4.125, -7.1447, 116.5)
 
 class Solver:
     def __init__(self, nx, ny, dx, gamma=1.4, *, precision=64, mode="exact", cons=False, force_hlle=True,
-                 jp_cri=(0.2, 1.0), cfl=0.5, bc="transmissive", bound=0, post=None, device=None):
+                 jp_cri=(0.2, 1.0), cfl=0.5, bc="transmissive", bound=0, post=None, device=None, weno_eps=1e-12):
         import torch
         if not torch.cuda.is_available():
             raise RuntimeError("Solver needs a CUDA GPU; there is no CPU fallback")
@@ -46,7 +46,7 @@ class Solver:
         _lib.check(self.L.weno_solver_create(
             ctypes.byref(h), self.nx, self.ny, self.dx, self.gamma, self.precision,
             _lib.FAST if mode == "fast" else _lib.EXACT, int(bool(cons)), int(bool(force_hlle)),
-            float(jp_cri[0]), float(jp_cri[1]), float(cfl), bc_kind, int(bound), post8.ctypes.data,
+            float(jp_cri[0]), float(jp_cri[1]), float(cfl), float(weno_eps), bc_kind, int(bound), post8.ctypes.data,
             self.stream.cuda_stream), "Solver")
         self._h = h
 
