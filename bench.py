@@ -401,13 +401,10 @@ def main():
         return run_c4(args)
 
     import torch
-    world, rank, local = dist_setup()
-    if world > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    else:
-        torch.cuda.set_device(0)
+    from weno_ext import replicas
+    world, rank, local = replicas.world()
+    torch.cuda.set_device(local if world > 1 else 0)
+    replicas.init("nccl")
     import weno_ext
     from weno_ext import _lib
     L = _lib.load()
@@ -424,8 +421,7 @@ def main():
     import ctypes
     _lib.check(L.weno_solver_enable_timing(s._h, 1), "timing")
     clocks = ClockSampler(torch.cuda.current_device())
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     clocks.start()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -435,21 +431,16 @@ def main():
     e1.record(s.stream)
     e1.synchronize()
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(e0.elapsed_time(e1), device="cuda")
     ms_cls = (ctypes.c_double * len(CLASSES))()
     n_cls = (ctypes.c_int64 * len(CLASSES))()
     _lib.check(L.weno_solver_timing_report(s._h, ms_cls, n_cls, len(CLASSES)), "timing report")
     _lib.check(L.weno_solver_enable_timing(s._h, 0), "timing")
     t_sim, nsteps_done, status = s.info()
     launches = s.launches_per_step * args.steps
-    value = nx * ny * args.steps * world / (ms / 1e3)
+    value = replicas.job_rate(nx * ny * args.steps, ms, world)
 
     # ---- dominant kernel and its roofline ----
     kern = {CLASSES[i]: {"ms": ms_cls[i], "launches": int(n_cls[i])} for i in range(len(CLASSES)) if n_cls[i]}
@@ -543,8 +534,7 @@ def main():
     if rank == 0:
         print(json.dumps(line))
     s.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finish()
     return 0
 
 

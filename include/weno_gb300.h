@@ -198,6 +198,24 @@ int weno_batch_info(weno_batch* b, int slot, double* t, int64_t* steps, int* act
 int weno_batch_poll(weno_batch* b, int* active, double* t, int64_t* steps);
 int weno_batch_stats(weno_batch* b, int64_t* ntiles, int64_t* free_cells, int* launches_per_step);
 
+/* ------------------------------------------------------------------------
+ * Device generators of the seeded initial data, written straight into a
+ * device array (nx+6, ny+6, 8) in the drivers' layout (no counterpart in the
+ * reference's extension; they restate Rie_prob_2d_rs.py:213-263 and
+ * unitest.py:169-205 with seeded states).
+ * ---------------------------------------------------------------------- */
+/* Four quadrants split at padded indices si, sj; prim16 = 4 x (rho, u, v, p)
+ * for (i<si, j<sj), (i>=si, j<sj), (i<si, j>=sj), (i>=si, j>=sj). */
+int weno_init_quadrant(double* out, int64_t nx, int64_t ny, int64_t si, int64_t sj, const double* prim16,
+                       double gamma, void* stream);
+/* Planar shock at angle theta through (x0, 0) on [0,lx]x[0,ly], Mach `mach`
+ * into gas at rest (rho1, p1), post-shock state from Rankine-Hugoniot, then
+ * the oblique-shock boundary; returns the boundary's bound row and 8-channel
+ * inflow vector for weno_solver_create / weno_batch_add. */
+int weno_init_oblique_shock(double* out, int64_t nx, int64_t ny, double lx, double ly, double x0, double mach,
+                            double theta, double rho1, double p1, double gamma, int64_t* bound_out, double* post8_out,
+                            void* stream);
+
 /* Diagnostics: measured FP64 FMA (TFLOP/s), FP64 divide (per s) and FP32 FMA
  * (TFLOP/s) throughput of the current device -- the compute-roofline
  * denominators, with no counterpart in the reference. */

@@ -46,6 +46,9 @@ SIGNATURES = {
     "weno_solver_timing_report": (_i, [_vp, ctypes.POINTER(_d), ctypes.POINTER(_i64), _i]),
     "weno_solver_launches_per_step": (_i, [_vp]),
     "weno_probe_rates": (_i, [ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d), _vp]),
+    "weno_init_quadrant": (_i, [_vp, _i64, _i64, _i64, _i64, _vp, _d, _vp]),
+    "weno_init_oblique_shock": (_i, [_vp, _i64, _i64, _d, _d, _d, _d, _d, _d, _d, _d, ctypes.POINTER(_i64), _vp,
+                                     _vp]),
     "weno_batch_tile_config_count": (_i, []),
     "weno_batch_create": (_i, [ctypes.POINTER(_vp), _i64, _i, _i, _i, _i, _i, _d, _d, _d, _d, _d, _i, _vp]),
     "weno_batch_destroy": (_i, [_vp]),

@@ -34,6 +34,7 @@ UNITS = {
     "probe.cu": [],
     "noalloc.cu": [],
     "batch.cu": ["--fmad=false"],
+    "init.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "batch_exact.cu": ["--fmad=false"],
     "batch_f64.cu": ["--fmad=true"],
     "batch_f32.cu": ["--fmad=true"],

@@ -35,6 +35,17 @@ def _conserve(q, gamma):
     return q
 
 
+def quadrant_states(seed):
+    """The four seeded primitive states (rho, u, v, p) of `quadrant`."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(4):
+        rho, p = rng.uniform(0.1, 2.0, 2)
+        u, v = rng.uniform(-1.0, 1.0, 2)
+        out.append((rho, u, v, p))
+    return out
+
+
 def quadrant(nx, ny, seed=0, gamma=GAMMA, split=0.5):
     rng = np.random.default_rng(seed)
     q = np.zeros((nx + 6, ny + 6, 8))
@@ -102,3 +113,32 @@ def batch_shapes(n, lo, hi, seed, max_aspect=4.0):
         if max(a, b) / min(a, b) <= max_aspect:
             out.append((int(round(a)), int(round(b))))
     return out
+
+
+def quadrant_device(nx, ny, seed=0, gamma=GAMMA, split=0.5):
+    """`quadrant` generated on the current CUDA device (a torch float64 tensor)."""
+    import ctypes
+    import torch
+    from . import _lib
+    L = _lib.load()
+    out = torch.empty((nx + 6, ny + 6, 8), dtype=torch.float64, device="cuda")
+    prim = np.ascontiguousarray(np.array(quadrant_states(seed), dtype=np.float64).reshape(16))
+    _lib.check(L.weno_init_quadrant(out.data_ptr(), nx, ny, 3 + int(split * nx), 3 + int(split * ny),
+                                    prim.ctypes.data, float(gamma), torch.cuda.current_stream().cuda_stream),
+               "init_quadrant")
+    return out
+
+
+def oblique_shock_device(nx, ny, lx, ly, mach, theta, x0=1.0 / 6.0, gamma=GAMMA):
+    """`oblique_shock` generated on the current CUDA device: (tensor, bound, post8)."""
+    import ctypes
+    import torch
+    from . import _lib
+    L = _lib.load()
+    out = torch.empty((nx + 6, ny + 6, 8), dtype=torch.float64, device="cuda")
+    bound = ctypes.c_int64()
+    post = np.zeros(8)
+    _lib.check(L.weno_init_oblique_shock(out.data_ptr(), nx, ny, float(lx), float(ly), float(x0), float(mach),
+                                         float(theta), 1.4, 1.0, float(gamma), ctypes.byref(bound), post.ctypes.data,
+                                         torch.cuda.current_stream().cuda_stream), "init_oblique_shock")
+    return out, bound.value, post

@@ -55,17 +55,19 @@ class Request:
     def cells(self):
         return self.nx * self.ny
 
-    def build(self):
-        """(q, dx, bc kwargs) of the request's initial data."""
+    def build(self, device=True):
+        """(q, dx, bc kwargs) of the request's initial data, generated on the GPU
+        (device=True) or with the numpy generators."""
         if self.init is not None:
             return self.init, 1.0 / max(self.nx, self.ny), dict(bc="transmissive")
         if self.kind == "shock":
             lx, ly = self.nx / max(self.nx, self.ny), self.ny / max(self.nx, self.ny)
-            q, bound, post = problems.oblique_shock(self.nx, self.ny, lx, ly, self.mach, self.theta, x0=lx / 24)
+            gen = problems.oblique_shock_device if device else problems.oblique_shock
+            q, bound, post = gen(self.nx, self.ny, lx, ly, self.mach, self.theta, x0=lx / 24)
             # the reference's oblique-shock driver steps at CFL 0.1 (double_mach_reflection.py:17)
             return q, lx / self.nx, dict(bc="dmr", bound=bound, post=post, cfl=0.1)
-        q = problems.quadrant(self.nx, self.ny, seed=self.seed)
-        return q, 1.0 / max(self.nx, self.ny), dict(bc="transmissive")
+        gen = problems.quadrant_device if device else problems.quadrant
+        return gen(self.nx, self.ny, seed=self.seed), 1.0 / max(self.nx, self.ny), dict(bc="transmissive")
 
 
 def footprint_bytes(nx, ny, precision):
