@@ -504,6 +504,7 @@ def main():
     if not args.no_variants:
         for name, vkw, k in (("fp64_exact", dict(kw, mode="exact"), max(2, args.steps // 3)),
                              ("fp32", dict(kw, precision=32, mode="fast"), args.steps * 4),
+                             ("df64", dict(kw, precision=48, mode="fast"), args.steps * 2),
                              ("fp64_fast_hllc_blend", dict(kw, force_hlle=False, jp_cri=(1e4, 1.1e4)),
                               max(2, args.steps // 2))):
             vms, vs = time_solver(weno_ext.Solver, q0, nx, ny, k, 3, **vkw)

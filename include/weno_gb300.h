@@ -121,8 +121,11 @@ int weno_l_local_host(const double* u, int64_t m, int64_t n, int64_t c, double d
  * Device-resident SSP-RK3 solver: the time loop of Rie_prob_2d_rs.py:169-207,
  * 311-365 (bc_kind WENO_BC_TRANSMISSIVE) or double_mach_reflection.py:97-134,
  * 229-260 (WENO_BC_DMR, unitest.py:207-227) with the state resident in HBM as
- * four conserved planes of (nx+6) x (ny+6).  precision 64 or 32 (the FP32
- * bulk variant computes dt in FP64).  The solver owns its device memory.
+ * four conserved planes of (nx+6) x (ny+6).  precision 64 (IEEE double), 48
+ * (double-float: pairs of floats with about 48 significant bits, run on the
+ * FP32 pipes, several times the FP64 rate on GB300) or 32 (FP32 bulk); dt,
+ * the positivity check and the conservation sums are FP64 in every mode.  The
+ * solver owns its device memory.
  * ---------------------------------------------------------------------- */
 enum { WENO_BC_TRANSMISSIVE = 0, WENO_BC_DMR = 1 };
 

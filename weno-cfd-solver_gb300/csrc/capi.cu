@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/weno_gb300.h"
+#include "df64.cuh"
 #include "errors.h"
 #include "launch_api.h"
 #include "step_ctl.h"
@@ -443,6 +444,7 @@ cudaError_t enqueue_step_t(weno_solver* s, int* launches) {
 
 cudaError_t enqueue_step(weno_solver* s, int* launches) {
   if (s->prec == 32) return enqueue_step_t<float, true>(s, launches);
+  if (s->prec == 48) return enqueue_step_t<df64, true>(s, launches);
   if (s->mode == WENO_FAST) return enqueue_step_t<double, true>(s, launches);
   return enqueue_step_t<double, false>(s, launches);
 }
@@ -475,7 +477,8 @@ int weno_solver_create(weno_solver** out, int64_t nx, int64_t ny, double dx, dou
   if (nx < 3 || ny < 3) return fail(WENO_ERR_SHAPE, "solver_create: nx, ny >= 3 required, got (%lld, %lld)",
                                     (long long)nx, (long long)ny);
   if (!force_hlle && (nx < 2 || ny < 2)) return fail(WENO_ERR_SHAPE, "solver_create: grid too small for the sensor");
-  if (precision != 64 && precision != 32) return fail(WENO_ERR_ARG, "solver_create: precision must be 64 or 32");
+  if (precision != 64 && precision != 32 && precision != 48)
+    return fail(WENO_ERR_ARG, "solver_create: precision must be 64, 48 (double-float) or 32");
   int rc;
   if ((rc = check_mode(mode))) return rc;
   if (bc_kind != WENO_BC_TRANSMISSIVE && bc_kind != WENO_BC_DMR)
@@ -483,7 +486,7 @@ int weno_solver_create(weno_solver** out, int64_t nx, int64_t ny, double dx, dou
   if (bc_kind == WENO_BC_DMR && !post8) return fail(WENO_ERR_ARG, "solver_create: DMR boundary needs post8");
   weno_solver* s = new weno_solver();
   s->prec = precision;
-  s->mode = precision == 32 ? WENO_FAST : mode;
+  s->mode = precision != 64 ? WENO_FAST : mode;
   s->cons = cons != 0;
   s->force_hlle = force_hlle != 0;
   s->jp_lo = jp_lo;
@@ -549,6 +552,7 @@ int weno_solver_set_state(weno_solver* s, const double* q, int64_t c, int64_t s0
   HostView v{q, s0, s1, s2};
   HostPlanes Q = state_planes(s, s->q);
   if (s->prec == 32) WENO_CK((Launch<float, true>::import_planes(v, s->M, s->N, Q, s->stream)));
+  else if (s->prec == 48) WENO_CK((Launch<df64, true>::import_planes(v, s->M, s->N, Q, s->stream)));
   else WENO_CK((Launch<double, false>::import_planes(v, s->M, s->N, Q, s->stream)));
   // Fresh clock; with primitive channels present the first dt comes from them.
   std::memset(s->ctl_host, 0, sizeof(StepCtl));
@@ -603,6 +607,7 @@ int weno_solver_get_state(weno_solver* s, double* out) {
   if (!s || !out) return fail(WENO_ERR_ARG, "solver_get_state: null argument");
   HostPlanes Q = state_planes(s, s->q);
   if (s->prec == 32) WENO_CK((Launch<float, true>::export_aos8(Q, s->M, s->N, s->gamma, out, s->stream)));
+  else if (s->prec == 48) WENO_CK((Launch<df64, true>::export_aos8(Q, s->M, s->N, s->gamma, out, s->stream)));
   else if (s->mode == WENO_FAST) WENO_CK((Launch<double, true>::export_aos8(Q, s->M, s->N, s->gamma, out, s->stream)));
   else WENO_CK((Launch<double, false>::export_aos8(Q, s->M, s->N, s->gamma, out, s->stream)));
   if (s->bc_kind == WENO_BC_DMR) {
@@ -640,6 +645,7 @@ int weno_solver_totals(weno_solver* s, double* out4) {
   d = s->staging;  // the first four doubles of the staging buffer
   const HostView v = state_view(s, s->q);
   if (s->prec == 32) WENO_CK((Launch<float, true>::totals(v, s->nx, s->ny, d, s->sm_count, s->stream)));
+  else if (s->prec == 48) WENO_CK((Launch<df64, true>::totals(v, s->nx, s->ny, d, s->sm_count, s->stream)));
   else WENO_CK((Launch<double, false>::totals(v, s->nx, s->ny, d, s->sm_count, s->stream)));
   WENO_CK(cudaMemcpyAsync(out4, d, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
   WENO_CK(cudaStreamSynchronize(s->stream));

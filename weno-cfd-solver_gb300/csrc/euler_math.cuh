@@ -16,6 +16,9 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
+
+#include "df64.cuh"
 
 #ifndef WENO_TU_NS
 #error "WENO_TU_NS names the translation unit's inline namespace (tu_exact or tu_fast)"
@@ -35,6 +38,14 @@ constexpr double kSqrt3_12 = 0.1443375673;  // truncated literal, not sqrt(3)/12
 constexpr double kGqA0 = 0.1928406937, kGqA1 = 0.6111111111, kGqA2 = 0.1960481952;
 constexpr double kC13 = 13.0 / 12.0;
 
+// Arithmetic kinds: native double takes the common-denominator WENO form (its
+// exponent range is ample); float and df64 (float exponent range) take the
+// reciprocal form.
+template <class T>
+constexpr bool is_native_f64 = std::is_same<T, double>::value;
+template <class T>
+constexpr bool is_f32 = std::is_same<T, float>::value;
+
 template <class T>
 __device__ __forceinline__ T vmax(T a, T b) { return fmax(a, b); }
 template <class T>
@@ -43,12 +54,12 @@ __device__ __forceinline__ T vmin(T a, T b) { return fmin(a, b); }
 // a / b: the IEEE quotient except in FAST float, which uses the SFU path.
 template <class T, bool FAST>
 __device__ __forceinline__ T qdiv(T a, T b) {
-  if constexpr (FAST && sizeof(T) == 4) return __fdividef(a, b);
+  if constexpr (FAST && is_f32<T>) return __fdividef(a, b);
   else return a / b;
 }
 template <class T, bool FAST>
 __device__ __forceinline__ T qrcp(T b) {
-  if constexpr (FAST && sizeof(T) == 4) return __fdividef(1.0f, b);
+  if constexpr (FAST && is_f32<T>) return __fdividef(1.0f, b);
   else return T(1.0) / b;
 }
 
@@ -157,7 +168,8 @@ __device__ __forceinline__ double pow2_scale_of(double x) {
 // with the three (eps+b_k) first scaled by the same power of two so that the
 // largest lies in [0.5, 1) -- the products then neither overflow nor lose the
 // dominant weight, whatever the magnitude of the stencil values.
-// FAST float: reciprocals, because FP32 would underflow the products.
+// FAST float and df64: reciprocals, because the float exponent range would
+// underflow the products.
 template <class T, bool FAST>
 __device__ __forceinline__ T weno_combine(T e0, T e1, T e2, T d0, T d1, T d2, T p0, T p1, T p2, T scale) {
   if constexpr (!FAST) {
@@ -168,7 +180,7 @@ __device__ __forceinline__ T weno_combine(T e0, T e1, T e2, T d0, T d1, T d2, T 
     const T w0 = a0 / sum, w1 = a1 / sum, w2 = a2 / sum;
     const T r = w0 * p0 + w1 * p1 + w2 * p2;
     return scale == T(1.0) ? r : r / scale;
-  } else if constexpr (sizeof(T) == 8) {
+  } else if constexpr (is_native_f64<T>) {
     const T sc = pow2_scale_of(fmax(fmax(e0, e1), e2));
     e0 *= sc;
     e1 *= sc;
@@ -241,7 +253,7 @@ __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& r
     const T g1 = (q3 - q1) * S;
     const T pa0 = q2 + g0 * S, pa1 = q2 - g1, pa2 = q2 - g2 * S;
     const T pb0 = q2 - g0 * S, pb1 = q2 + g1, pb2 = q2 + g2 * S;
-    if constexpr (sizeof(T) == 8) {
+    if constexpr (is_native_f64<T>) {
       const T sc = pow2_scale_of(fmax(fmax(e0, e1), e2));
       const T f0 = e0 * sc, f1 = e1 * sc, f2 = e2 * sc;
       const T s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;

@@ -53,7 +53,35 @@ __global__ void __launch_bounds__(128) k_pass1(CView<T> u, int64_t rows, int64_t
 #pragma unroll
     for (int k = 0; k < 4; ++k) c[s][k] = Y ? u.at(row, col + s, k) : u.at(row + s, col, k);
   T ql[4], qr[4];
-  pass1_face<T, FAST, Y, CHAR>(c, gamma, ql, qr, weps);
+  if constexpr (std::is_same<T, df64>::value) {
+    // df64 has the float exponent range: a face whose stencil holds a tiny
+    // density or a huge value (near vacuum the characteristic projection scales
+    // by 1/(rho*c)) is reconstructed in native double instead.
+    bool safe = true;
+#pragma unroll
+    for (int s = 0; s < 6; ++s) {
+      safe = safe && c[s][0].hi > 1e-6f;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) safe = safe && fabsf(c[s][k].hi) < 1e15f;
+    }
+    if (safe) {
+      pass1_face<T, FAST, Y, CHAR>(c, gamma, ql, qr, weps);
+    } else {
+      double cd[6][4], l[4], r[4];
+#pragma unroll
+      for (int s = 0; s < 6; ++s)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) cd[s][k] = (double)c[s][k];
+      pass1_face<double, FAST, Y, CHAR>(cd, (double)gamma, l, r, (double)weps);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        ql[k] = T(l[k]);
+        qr[k] = T(r[k]);
+      }
+    }
+  } else {
+    pass1_face<T, FAST, Y, CHAR>(c, gamma, ql, qr, weps);
+  }
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     PL.at(k, row, col) = ql[k];

@@ -24,6 +24,9 @@ struct HostPlanes {
 };
 
 struct StepCtl;
+namespace dfm {
+struct df64;
+}
 
 template <class T, bool FAST>
 struct Launch {
@@ -72,5 +75,6 @@ cudaError_t launch_run_begin(StepCtl* ctl, double t_final, long long add, cudaSt
 extern template struct Launch<double, false>;
 extern template struct Launch<double, true>;
 extern template struct Launch<float, true>;
+extern template struct Launch<dfm::df64, true>;
 
 }  // namespace weno

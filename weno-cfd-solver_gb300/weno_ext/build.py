@@ -30,6 +30,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"] + ARCH
 UNITS = {
     "tu_exact.cu": ["--fmad=false"],
     "tu_fast.cu": ["--fmad=true"],
+    "tu_df64.cu": ["--fmad=true"],
     "capi.cu": [],
     "probe.cu": [],
     "noalloc.cu": [],

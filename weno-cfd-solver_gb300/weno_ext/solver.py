@@ -34,7 +34,8 @@ class Solver:
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.nx, self.ny, self.dx, self.gamma = int(nx), int(ny), float(dx), float(gamma)
         self.M, self.N = self.nx + 6, self.ny + 6
-        self.precision = int(precision)
+        self.precision = {"df64": 48, "f64": 64, "f32": 32}.get(precision, precision)
+        self.precision = int(self.precision)
         self.bc = bc
         bc_kind = {"transmissive": _lib.BC_TRANSMISSIVE, "dmr": _lib.BC_DMR}[bc]
         post8 = np.ascontiguousarray(DMR_POST if post is None else post, dtype=np.float64)
