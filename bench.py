@@ -381,6 +381,9 @@ def main():
     ap.add_argument("--nx", type=int, default=4096)
     ap.add_argument("--ny", type=int, default=4096)
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--precision", default="f64", choices=["f64", "df64", "f32"],
+                    help="arithmetic of the headline solver (f64 = IEEE double, the default; df64 = double-float "
+                         "pairs on the FP32 pipes; f32)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -411,7 +414,8 @@ def main():
 
     nx, ny = args.nx, args.ny
     q0 = quadrant_state(nx, ny)
-    kw = dict(precision=64, mode=args.mode, cons=False, force_hlle=True, jp_cri=(0.2, 1.0), cfl=0.45)
+    prec_code = {"f64": 64, "df64": 48, "f32": 32}[args.precision]
+    kw = dict(precision=prec_code, mode=args.mode, cons=False, force_hlle=True, jp_cri=(0.2, 1.0), cfl=0.45)
     s = weno_ext.Solver(nx, ny, 1.0 / nx, GAMMA, **kw)
     s.set_state(q0)
     s.run(args.warmup, graph=False)
@@ -446,7 +450,7 @@ def main():
     kern = {CLASSES[i]: {"ms": ms_cls[i], "launches": int(n_cls[i])} for i in range(len(CLASSES)) if n_cls[i]}
     dom = max(kern, key=lambda k: kern[k]["ms"])
     M, N = nx + 6, ny + 6
-    es = 8
+    es = 4 if args.precision == "f32" else 8
     # Algorithmic bytes per launch: the stencil input once plus the outputs once.
     alg_bytes = {
         "pass1_x": (4 * M * N + 8 * (M - 5) * N) * es,
@@ -461,6 +465,8 @@ def main():
     achieved = alg_bytes.get(dom, 0) / (per_launch_ms / 1e3) / 1e9 if dom in alg_bytes else None
     prof = load_json(os.path.join(ROOT, "profiles", "roofline_traffic.json")) or {}
     traffic = prof.get(dom, {}).get("dram_bytes_per_launch") if isinstance(prof.get(dom), dict) else None
+    if args.precision != "f64":
+        traffic = None  # the committed DRAM capture is of the FP64 kernels
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"}
@@ -469,7 +475,7 @@ def main():
     flops = load_json(os.path.join(ROOT, "profiles", "flops_per_cell.json")) or {}
     fpc = flops.get("char_hlle_step")
     compute = None
-    if fpc and r64.value > 0:
+    if fpc and r64.value > 0 and args.precision == "f64":
         ach = fpc * value / world / 1e12
         compute = {"bound": "fp64", "achieved": ach, "peak": r64.value, "unit": "TFLOP/s",
                    "frac": ach / r64.value, "flops_per_cell_update": fpc,
@@ -514,9 +520,9 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
         "config": {"workload": f"four-quadrant Riemann {nx}x{ny}, char-WENO5 + 2-pt Gauss faces + HLLE, "
-                               f"SSP-RK3, CFL 0.45, FP64 ({args.mode} arithmetic)",
+                               f"SSP-RK3, CFL 0.45, {args.precision} ({args.mode} arithmetic)",
                    "nx": nx, "ny": ny, "seed": SEED, "mode": args.mode,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (state 4 x (nx+6)(ny+6) f64 = %.0f MB per buffer)" %
