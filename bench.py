@@ -287,7 +287,7 @@ def run_c3(args):
     sample = states[:: max(1, len(states) // 64)]
     cfg, tune = autotune.best_tile_config(sample, **kw)
     cells = sum(nx * ny for nx, ny in shapes)
-    b = weno_ext.Batch(cells + 64 * len(shapes) + 4096, len(shapes), tile_config=cfg, **kw)
+    b = weno_ext.Batch(weno_ext.Batch.pool_cells(shapes, 32), len(shapes), tile_config=cfg, **kw)
     slots = [b.add(q, dx, t_end=float(te)) for (q, dx), te in zip(states, t_ends)]
     b.run(1)
     b.synchronize()
@@ -311,6 +311,10 @@ def run_c3(args):
     act, tt, nn = b.poll()
     cu = int(sum(nx * ny * (int(n) - int(d)) for (nx, ny), n, d in zip(shapes, nn, done_before)))
     st = b.stats()
+    # Solves the reference scheme itself drives non-finite (component-wise WENO5 has no
+    # positivity limiter) stop with a numeric status; the others must reach t_end.
+    failed = [k for k, sl in enumerate(slots) if b.info(sl)["status"] != 0]
+    ok = [k for k in range(len(slots)) if k not in set(failed)]
     line = {
         "metric": "aggregate cell-updates/s, batched uneven four-quadrant solves (FP32)", "config_name": "c3",
         "value": cu / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "dtype": "f32", "data": "synthetic",
@@ -320,7 +324,8 @@ def run_c3(args):
         "steps_replayed": graph_steps, "cell_updates": cu, "gpu_ms": ms, "wall_s": wall,
         "launches_per_step": st["launches_per_step"],
         "max_steps_of_a_solve": int(nn.max()), "min_steps_of_a_solve": int(nn.min()),
-        "t_end_reached": bool(np.all(np.abs(tt - t_ends) < 1e-9)),
+        "solves_nonfinite": len(failed),
+        "t_end_reached_by_the_others": bool(np.all(np.abs(tt[ok] - t_ends[ok]) < 1e-9)),
     }
     print(json.dumps(line))
     b.close()

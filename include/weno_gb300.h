@@ -196,6 +196,8 @@ int weno_batch_remove(weno_batch* b, int slot);
 int weno_batch_run(weno_batch* b, int64_t nsteps, int use_graph);
 /* The driver's (nx+6, ny+6, 8) array of one solve (device pointer); synchronises. */
 int weno_batch_get_state(weno_batch* b, int slot, double* out);
+/* status: WENO_OK, WENO_ERR_NUMERIC (a non-finite wave speed stopped the solve) or
+ * WENO_ERR_CUDA (a tile's staging copy did not complete within its time limit). */
 int weno_batch_info(weno_batch* b, int slot, double* t, int64_t* steps, int* active, int* status);
 /* Synchronise and copy every slot's active flag, time and step count (arrays of max_solves). */
 int weno_batch_poll(weno_batch* b, int* active, double* t, int64_t* steps);

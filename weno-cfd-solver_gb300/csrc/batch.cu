@@ -1,12 +1,14 @@
 // C ABI of the batched solver (include/weno_gb300.h, weno_batch_*).
 //
 // A batch owns one packed pool per RK buffer (state, stage 1, stage 2) of a
-// fixed capacity, a table of solve descriptors and per-solve clocks, and a tile
-// list.  Solves join (weno_batch_add) and leave (weno_batch_remove) between
-// runs; the pool is first-fit allocated on the host.  The device-side tables
+// fixed capacity, carved from one allocation, a table of solve descriptors,
+// per-solve clocks and TMA tensor maps, and a tile list.  Solves join
+// (weno_batch_add) and leave (weno_batch_remove) between runs; the pool is
+// first-fit allocated on the host.  The device-side tables
 // keep their addresses for the batch's lifetime, so a captured step graph stays
 // valid while membership changes; the tile count is the only launch argument
 // that changes, and a change re-captures the graph.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -44,6 +46,23 @@ int bfail(int code, const char* fmt, ...) {
 
 inline long long align64(long long x) { return (x + 63) / 64 * 64; }
 
+// cuTensorMapEncodeTiled, fetched once through the runtime (no link against libcuda).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
 }  // namespace
 
 struct weno_batch {
@@ -58,7 +77,10 @@ struct weno_batch {
   bool own_stream = false;
   int sm_count = 152;
   int occ = 1;  // resident CTAs per SM of the stage kernel
+  void* pool_base = nullptr;  // the three pools, `capacity` elements apart
   void* pool[3] = {nullptr, nullptr, nullptr};
+  CUtensorMap* d_tmaps = nullptr;  // one per slot: (column, row, plane, pool) of that solve
+  std::vector<CUtensorMap> h_tmaps;
   SolveDesc* d_solves = nullptr;
   SolveCtl* d_ctl = nullptr;
   std::vector<SolveDesc> h_solves;
@@ -87,10 +109,10 @@ cudaError_t enqueue_batch_step(weno_batch* b) {
   cudaError_t e;
   if ((e = BL::clock(b->d_ctl, b->max_solves, 0, b->stream))) return e;
   for (int s = 1; s <= 3; ++s) {
-    const void* qin = b->pool[s == 1 ? 0 : (s == 2 ? 1 : 2)];
+    // stage s reads pool s-1 (q, q1, q2) through the tensor maps
     void* qo = b->pool[s == 1 ? 1 : (s == 2 ? 2 : 0)];
-    if ((e = BL::stage(b->cfg, b->chr, b->blend, b->d_solves, b->d_ctl, b->d_tiles, b->ntiles, grid, qin, b->pool[0],
-                       qo, s, b->gamma, b->jp_lo, b->jp_hi, b->weps, b->stream)))
+    if ((e = BL::stage(b->cfg, b->chr, b->blend, b->d_solves, b->d_ctl, b->d_tiles, b->ntiles, grid, b->d_tmaps,
+                       b->pool[0], qo, s, b->gamma, b->jp_lo, b->jp_hi, b->weps, b->stream)))
       return e;
   }
   return BL::clock(b->d_ctl, b->max_solves, 1, b->stream);
@@ -174,16 +196,27 @@ void pool_free(weno_batch* b, long long off, long long len) {
   }
 }
 
+// Installs a host-encoded tensor map (passed by value) at `dst` in global
+// memory and releases it to the tensormap proxy; the stage kernel acquires it.
+__global__ void k_install_tensormap(CUtensorMap* dst, const __grid_constant__ CUtensorMap src) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const uint4* s = reinterpret_cast<const uint4*>(&src);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+#pragma unroll
+  for (int k = 0; k < (int)(sizeof(CUtensorMap) / sizeof(uint4)); ++k) d[k] = s[k];
+  tma::tensormap_release(dst);
+}
+
 // Import a padded (nx+6, ny+6, c) array into a solve's interior planes.
 template <class T>
 __global__ void k_import_interior(const double* q, long long s0, long long s1, long long s2, int nx, int ny, T* dst,
-                                  long long ps) {
+                                  long long ps, int ld) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= nx || j >= ny) return;
+  if (i >= nx || j >= ld) return;
   const double* c = q + (long long)(i + 3) * s0 + (long long)(j + 3) * s1;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) dst[k * ps + (long long)i * ny + j] = (T)c[k * s2];
+  for (int k = 0; k < 4; ++k) dst[k * ps + (long long)i * ld + j] = j < ny ? (T)c[k * s2] : T(0);
 }
 
 // Export a solve as the driver's (nx+6, ny+6, 8) array: ghost cells from the
@@ -205,7 +238,7 @@ __global__ void k_export_solve(const SolveDesc* solves, int slot, const T* pool,
   }
   double q[4];
   {
-    const long long o = d.off + (long long)g.i * d.ny + g.j;
+    const long long o = d.off + (long long)g.i * d.ld + g.j;
     for (int k = 0; k < 4; ++k) q[k] = (double)pool[o + k * d.ps];
     if (g.flip2) q[2] = -q[2];
   }
@@ -219,7 +252,8 @@ __global__ void k_export_solve(const SolveDesc* solves, int slot, const T* pool,
 void batch_free(weno_batch* b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
-  for (void* p : b->pool) cudaFree(p);
+  cudaFree(b->pool_base);
+  cudaFree(b->d_tmaps);
   cudaFree(b->d_solves);
   cudaFree(b->d_ctl);
   cudaFree(b->d_tiles);
@@ -283,8 +317,14 @@ int weno_batch_create(weno_batch** out, int64_t pool_cells, int max_solves, int 
   b->occ = std::max(1, precision == 32 ? BatchLaunch<float, true>::ctas_per_sm(b->cfg, b->chr, b->blend)
                        : (b->mode == WENO_FAST ? BatchLaunch<double, true>::ctas_per_sm(b->cfg, b->chr, b->blend)
                                                : BatchLaunch<double, false>::ctas_per_sm(b->cfg, b->chr, b->blend)));
-  for (int k = 0; k < 3; ++k)
-    if ((e = cudaMalloc(&b->pool[k], (size_t)b->capacity * b->es))) return bail(e, "cudaMalloc(pool)");
+  if (!encode_tiled()) {
+    batch_free(b);
+    return bfail(WENO_ERR_CUDA, "batch_create: cuTensorMapEncodeTiled is not available from the driver");
+  }
+  if ((e = cudaMalloc(&b->pool_base, 3 * (size_t)b->capacity * b->es))) return bail(e, "cudaMalloc(pool)");
+  for (int k = 0; k < 3; ++k) b->pool[k] = static_cast<char*>(b->pool_base) + (size_t)k * b->capacity * b->es;
+  if ((e = cudaMalloc(&b->d_tmaps, sizeof(CUtensorMap) * max_solves))) return bail(e, "cudaMalloc(tensor maps)");
+  b->h_tmaps.assign(max_solves, CUtensorMap{});
   if ((e = cudaMalloc(&b->d_solves, sizeof(SolveDesc) * max_solves))) return bail(e, "cudaMalloc(solves)");
   if ((e = cudaMalloc(&b->d_ctl, sizeof(SolveCtl) * max_solves))) return bail(e, "cudaMalloc(ctl)");
   if ((e = cudaMallocHost(&b->h_ctl, sizeof(SolveCtl) * max_solves))) return bail(e, "cudaMallocHost(ctl)");
@@ -322,14 +362,38 @@ int weno_batch_add(weno_batch* b, int64_t nx, int64_t ny, double dx, int bc_kind
       break;
     }
   if (slot < 0) return bfail(WENO_ERR_WORKSPACE, "batch_add: all %d solve slots are in use", b->max_solves);
-  const long long ps = align64(nx * ny);
+  const int lq = (int)(16 / b->es);  // row pitch quantum: 16 bytes
+  const long long ld = (ny + lq - 1) / lq * lq;
+  const long long ps = align64(nx * ld);
   const long long off = pool_alloc(b, 4 * ps);
   if (off < 0) return bfail(WENO_ERR_WORKSPACE, "batch_add: pool full (%lld cells requested)", (long long)(nx * ny));
+  // Tensor map of this solve over all three pools: dims (column, row, plane, pool).
+  {
+    unsigned bc = 0, br = 0;
+    if (b->prec == 32) BatchLaunch<float, true>::box(b->cfg, b->blend, &bc, &br);
+    else BatchLaunch<double, true>::box(b->cfg, b->blend, &bc, &br);
+    const cuuint64_t dims[4] = {(cuuint64_t)ny, (cuuint64_t)nx, 4, 3};
+    const cuuint64_t strides[3] = {(cuuint64_t)(ld * b->es), (cuuint64_t)(ps * b->es),
+                                   (cuuint64_t)(b->capacity * b->es)};
+    const cuuint32_t box[4] = {bc, br, 4, 1};
+    const cuuint32_t elem[4] = {1, 1, 1, 1};
+    void* base = static_cast<char*>(b->pool_base) + (size_t)off * b->es;
+    const CUresult r = encode_tiled()(&b->h_tmaps[slot],
+                                      b->prec == 32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                                      4, base, dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      pool_free(b, off, 4 * ps);
+      return bfail(WENO_ERR_CUDA, "batch_add: cuTensorMapEncodeTiled failed (%d)", (int)r);
+    }
+  }
   SolveDesc d{};
   d.off = off;
   d.ps = ps;
   d.nx = (int)nx;
   d.ny = (int)ny;
+  d.ld = (int)ld;
   d.bc = bc_kind;
   d.bound = (int)bound;
   d.dx = dx;
@@ -338,15 +402,17 @@ int weno_batch_add(weno_batch* b, int64_t nx, int64_t ny, double dx, int bc_kind
   b->h_solves[slot] = d;
   b->used[slot] = true;
   WB_CK(cudaMemcpyAsync(b->d_solves + slot, &b->h_solves[slot], sizeof(SolveDesc), cudaMemcpyHostToDevice, b->stream));
-  // interior state
+  k_install_tensormap<<<1, 32, 0, b->stream>>>(b->d_tmaps + slot, b->h_tmaps[slot]);
+  WB_CK(cudaGetLastError());
+  // interior state (the row padding is zeroed)
   const dim3 blk(32, 4);
-  const dim3 grd((unsigned)((ny + 31) / 32), (unsigned)((nx + 3) / 4));
+  const dim3 grd((unsigned)((ld + 31) / 32), (unsigned)((nx + 3) / 4));
   if (b->prec == 32)
     k_import_interior<float><<<grd, blk, 0, b->stream>>>(q, s0, s1, s2, (int)nx, (int)ny,
-                                                        static_cast<float*>(b->pool[0]) + off, ps);
+                                                        static_cast<float*>(b->pool[0]) + off, ps, (int)ld);
   else
     k_import_interior<double><<<grd, blk, 0, b->stream>>>(q, s0, s1, s2, (int)nx, (int)ny,
-                                                         static_cast<double*>(b->pool[0]) + off, ps);
+                                                         static_cast<double*>(b->pool[0]) + off, ps, (int)ld);
   WB_CK(cudaGetLastError());
   // clock
   SolveCtl& cc = b->h_ctl[slot];
@@ -449,7 +515,7 @@ int weno_batch_info(weno_batch* b, int slot, double* t, int64_t* steps, int* act
   if (t) *t = c.t;
   if (steps) *steps = c.steps;
   if (active) *active = b->used[slot] ? c.active : 0;
-  if (status) *status = c.status ? WENO_ERR_NUMERIC : WENO_OK;
+  if (status) *status = (c.status & 4) ? WENO_ERR_CUDA : (c.status ? WENO_ERR_NUMERIC : WENO_OK);
   return WENO_OK;
 }
 

@@ -17,12 +17,14 @@ constexpr int kTileTY[kNumTileConfigs] = {32, 32, 16, 64};
 
 template <class T, bool FAST>
 struct BatchLaunch {
+  // TMA box of one tile: columns (innermost, also the shared-memory row pitch) and rows.
+  static void box(int cfg, bool blend, unsigned* cols, unsigned* rows);
   // Shared memory bytes of one CTA, or 0 if the configuration does not fit.
   static size_t smem_bytes(int cfg, bool blend);
   // Resident CTAs per SM for the configuration (0 if it cannot launch).
   static int ctas_per_sm(int cfg, bool chr, bool blend);
   static cudaError_t stage(int cfg, bool chr, bool blend, const SolveDesc* solves, SolveCtl* ctl, const void* tiles,
-                           int ntiles, int grid, const void* qin, const void* qn, void* qo, int stage, double gamma,
+                           int ntiles, int grid, const void* tmaps, const void* qn, void* qo, int stage, double gamma,
                            double jp_lo, double jp_hi, double weps, cudaStream_t st);
   static cudaError_t cfl(int cfg, const SolveDesc* solves, SolveCtl* ctl, const void* tiles, int ntiles, int grid,
                          const void* q, double gamma, cudaStream_t st);

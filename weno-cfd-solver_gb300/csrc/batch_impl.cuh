@@ -17,8 +17,9 @@ constexpr size_t tile_smem() {
 }
 
 template <class T, bool FAST, bool CHAR, bool BLEND, int TX, int TY>
-cudaError_t launch_stage(const SolveDesc* solves, SolveCtl* ctl, const int4* tiles, int ntiles, int grid, const T* qin,
-                         const T* qn, T* qo, int stage, T gamma, T jp_lo, T jp_hi, T weps, cudaStream_t st) {
+cudaError_t launch_stage(const SolveDesc* solves, SolveCtl* ctl, const int4* tiles, int ntiles, int grid,
+                         const CUtensorMap* tmaps, const T* qn, T* qo, int stage, T gamma, T jp_lo, T jp_hi, T weps,
+                         cudaStream_t st) {
   constexpr size_t sm = tile_smem<T, TX, TY, BLEND>();
   if constexpr (sm > 227 * 1024) {
     return cudaErrorInvalidConfiguration;
@@ -30,7 +31,7 @@ cudaError_t launch_stage(const SolveDesc* solves, SolveCtl* ctl, const int4* til
       if (e != cudaSuccess) return e;
       attr_set = true;
     }
-    k<<<grid, kNT, sm, st>>>(solves, ctl, tiles, ntiles, qin, qn, qo, stage, gamma, jp_lo, jp_hi, weps);
+    k<<<grid, kNT, sm, st>>>(solves, ctl, tiles, ntiles, tmaps, qn, qo, stage, gamma, jp_lo, jp_hi, weps);
     return cudaGetLastError();
   }
 }
@@ -61,6 +62,15 @@ int occupancy() {
   }
 
 template <class T, bool FAST>
+void BatchLaunch<T, FAST>::box(int cfg, bool blend, unsigned* cols, unsigned* rows) {
+#define WENO_BOX(TX, TY)                                      \
+  *cols = (unsigned)TileGeom<TX, TY, false>::UC;              \
+  *rows = blend ? (unsigned)TileGeom<TX, TY, true>::UR : (unsigned)TileGeom<TX, TY, false>::UR;
+  WENO_TILE_SWITCH(cfg, WENO_BOX)
+#undef WENO_BOX
+}
+
+template <class T, bool FAST>
 size_t BatchLaunch<T, FAST>::smem_bytes(int cfg, bool blend) {
   size_t r = 0;
 #define WENO_SM(TX, TY) \
@@ -85,12 +95,12 @@ int BatchLaunch<T, FAST>::ctas_per_sm(int cfg, bool chr, bool blend) {
 
 template <class T, bool FAST>
 cudaError_t BatchLaunch<T, FAST>::stage(int cfg, bool chr, bool blend, const SolveDesc* solves, SolveCtl* ctl,
-                                        const void* tiles, int ntiles, int grid, const void* qin, const void* qn,
+                                        const void* tiles, int ntiles, int grid, const void* tmaps, const void* qn,
                                         void* qo, int stage, double gamma, double jp_lo, double jp_hi,
                                         double weps, cudaStream_t st) {
   if (ntiles <= 0 || grid <= 0) return cudaSuccess;
   const int4* tl = static_cast<const int4*>(tiles);
-  const T* a = static_cast<const T*>(qin);
+  const CUtensorMap* a = static_cast<const CUtensorMap*>(tmaps);
   const T* b = static_cast<const T*>(qn);
   T* o = static_cast<T*>(qo);
   cudaError_t e = cudaSuccess;

@@ -1,17 +1,20 @@
 // Batched solver: many independent 2-D problems of uneven size stepped together.
 //
 // Pool layout.  Every solve stores only its interior cells, as four conserved
-// planes of nx x ny (row stride ny, plane stride `ps`) at element offset `off`
-// of a packed pool; the pool exists three times (current state, stage 1,
-// stage 2) with identical offsets.  Ghost cells are never stored: a tile
-// loader resolves each ghost index to the interior cell (or inflow constant)
-// the boundary fill would have copied there (Rie_prob_2d_rs.py:123-152,
+// planes of nx rows (row pitch `ld` = ny rounded up to 16 bytes, plane stride
+// `ps`) at element offset `off` of a packed pool; the pool exists three times
+// (current state, stage 1, stage 2) in one allocation, with identical offsets,
+// so one 4-D tensor map per solve (column, row, plane, pool) addresses all of
+// it.  Ghost cells are never stored: after the tile is staged, each ghost cell
+// of the tile is filled from the interior cell (or inflow constant) the
+// boundary fill would have copied there (Rie_prob_2d_rs.py:123-152,
 // unitest.py:207-227), so the fill costs no pass of its own.
 //
 // Work.  The unit is a tile of TX x TY interior cells of one solve.  A packed
 // tile list (solve, i0, j0) covers every active solve; one persistent kernel
-// per RK stage walks it.  A CTA loads the tile plus its halo into shared
-// memory, runs pass 1 (normal WENO5), pass 2 (Gauss-quadrature WENO, fluxes,
+// per RK stage walks it.  A CTA stages the tile plus its halo into shared
+// memory with one TMA box load (cp.async.bulk.tensor, completion on an
+// mbarrier), runs pass 1 (normal WENO5), pass 2 (Gauss-quadrature WENO, fluxes,
 // Riemann solver), the sensor blend and the flux difference fused with the
 // SSP-RK3 stage combination, and writes the tile of the next stage state.
 // Stage 3 also reduces the new state's wave speed per solve for the next dt.
@@ -19,6 +22,7 @@
 
 #include "euler_math.cuh"
 #include "step_ctl.h"
+#include "tma.cuh"
 
 namespace weno {
 
@@ -26,6 +30,7 @@ struct SolveDesc {
   long long off;  // element offset of plane 0 in each pool
   long long ps;   // plane stride (elements)
   int nx, ny;
+  int ld;         // row pitch (elements): ny rounded up to a multiple of 16 bytes
   int bc;         // 0 transmissive (mirror), 1 oblique-shock / DMR segments
   int bound;      // DMR: last row of the inflow segment on the lower boundary
   double dx;      // cell size (dx = dy)
@@ -36,7 +41,7 @@ struct SolveCtl {
   double t, t_end, dt, cfl_dx;
   unsigned long long cmax_bits;
   int active;      // 0: finished (t >= t_end - 1e-12 or step cap) or not admitted
-  int status;      // 1: non-finite wave speed
+  int status;      // 1: non-finite wave speed; 4: a tile's staging copy did not land
   long long steps, max_steps;
 };
 
@@ -98,7 +103,12 @@ template <int TX, int TY, bool BLEND>
 struct TileGeom {
   static constexpr int HF = BLEND ? 1 : 0;     // extra face halo for the sensor stencil
   static constexpr int UR = TX + 6 + 2 * HF;   // tile rows incl. halo
-  static constexpr int UC = TY + 6 + 2 * HF;
+  static constexpr int UCV = TY + 6 + 2 * HF;  // tile columns incl. halo
+  // The staged box starts at column j0 - 4 (a 16-byte boundary, j0 being a
+  // multiple of TY): halo column c of the tile sits at box column c + CO, and
+  // the box is TY + 8 columns wide, which is also the shared-memory row pitch.
+  static constexpr int CO = 1 - HF;
+  static constexpr int UC = TY + 8;
   static constexpr int P1XR = TX + 1 + 2 * HF, P1XC = TY + 4 + 2 * HF;  // pass-1 x faces x columns
   static constexpr int P1YR = TX + 4 + 2 * HF, P1YC = TY + 1 + 2 * HF;  // pass-1 rows x y faces
   static constexpr int P1 = (P1XR * P1XC > P1YR * P1YC) ? P1XR * P1XC : P1YR * P1YC;
@@ -132,21 +142,32 @@ __device__ __forceinline__ T tile_sensor(const T* pbar, int R, int C, int fr, in
   return sensor_weight<T, FAST>(dpdx, dpdy, p, jp_lo, jp_hi);
 }
 
-// One SSP-RK3 stage (STAGE 1..3) for every tile of the list.  Qin is the stage
-// input pool (q, q1, q2), Qn the step's initial state, Qo the output pool.
+// One SSP-RK3 stage (1..3) for every tile of the list.  The stage input (pool
+// stage-1 of q, q1, q2) is read through each solve's tensor map `tmaps[solve]`;
+// Qn is the step's initial state, Qo the output pool.
 template <class T, bool FAST, bool CHAR, bool BLEND, int TX, int TY, int NT>
 __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict__ solves, SolveCtl* ctl,
-                                                     const int4* __restrict__ tiles, int ntiles, const T* Qin,
-                                                     const T* Qn, T* Qo, int stage, T gamma, T jp_lo, T jp_hi,
-                                                     T weps) {
+                                                     const int4* __restrict__ tiles, int ntiles,
+                                                     const CUtensorMap* tmaps, const T* Qn, T* Qo, int stage,
+                                                     T gamma, T jp_lo, T jp_hi, T weps) {
   using G = TileGeom<TX, TY, BLEND>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  static_assert(G::UC * sizeof(T) % 16 == 0, "box rows must be whole 16-byte units");
+  constexpr uint32_t kBoxBytes = (uint32_t)(sizeof(T) * G::U_ELEMS);
+  constexpr uint64_t kWaitNs = 1000000000ull;  // 1 s
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   T* U = reinterpret_cast<T*>(smem_raw);
   T* P1 = U + G::U_ELEMS;
   T* FX = P1 + G::P1_ELEMS;
   T* FY = FX + G::FX_ELEMS;
   __shared__ double red[NT / 32];
+  __shared__ uint64_t bar;
   const int tid = threadIdx.x;
+  if (tid == 0) {
+    tma::mbar_init(&bar, 1);
+    tma::fence_mbar_init();
+  }
+  __syncthreads();
+  uint32_t phase = 0;
 
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int4 tl = tiles[t];
@@ -154,29 +175,53 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
     if (!ctl[tl.x].active) continue;  // uniform across the CTA
     const int i0 = tl.y, j0 = tl.z;
     const int nx = d.nx, ny = d.ny;
-    const T* qin = Qin + d.off;
     const long long ps = d.ps;
     const int HF = G::HF;
 
-    // ---- load the tile and its halo, resolving ghost cells ----
-    for (int e = tid; e < G::UR * G::UC; e += NT) {
-      const int r = e / G::UC, c = e % G::UC;
+    // ---- stage the tile and its halo: one TMA box of (TY+8) x UR x 4 planes
+    // from the stage-input pool (stage-1); cells outside the solve read 0 ----
+    {
+      const CUtensorMap* tm = tmaps + tl.x;
+      if (tid == 0) {
+        tma::tensormap_acquire(tm);
+        tma::mbar_arrive_expect_tx(&bar, kBoxBytes);
+        tma::load_4d(U, tm, j0 - 4, i0 - HF - 3, 0, stage - 1, &bar);
+      }
+      const uint32_t par = phase;
+      phase ^= 1u;
+      const bool landed = tma::mbar_wait_bounded(&bar, par, kWaitNs);
+      if (!__syncthreads_and(landed)) {
+        if (tid == 0) atomicOr(&ctl[tl.x].status, 4);
+        tma::mbar_wait_bounded(&bar, par, kWaitNs);  // let a late copy land before the CTA leaves
+        return;
+      }
+    }
+    // ---- ghost cells of the tile from the staged interior ----
+    for (int e = tid; e < G::UR * G::UCV; e += NT) {
+      const int r = e / G::UCV, c = e % G::UCV;
       const int I = i0 - HF + r, J = j0 - HF + c;  // padded coordinates
-      T v[4] = {T(0), T(0), T(0), T(0)};
-      if (I >= 0 && I < nx + 6 && J >= 0 && J < ny + 6) {
-        const GhostSrc g = resolve_cell(d, I, J);
-        if (g.post) {
+      if (I < 0 || I >= nx + 6 || J < 0 || J >= ny + 6) continue;
+      if (I >= 3 && I < nx + 3 && J >= 3 && J < ny + 3) continue;
+      const GhostSrc g = resolve_cell(d, I, J);
+      T v[4];
+      if (g.post) {
 #pragma unroll
-          for (int k = 0; k < 4; ++k) v[k] = T(d.post[k]);
+        for (int k = 0; k < 4; ++k) v[k] = T(d.post[k]);
+      } else {
+        const int sr = g.i + 3 - (i0 - HF), sc = g.j + 3 - (j0 - HF);
+        if (sr < 0 || sr >= G::UR || sc < 0 || sc >= G::UCV) {
+          // not reachable for tiles that start inside their solve; kept as a checked fallback
+#pragma unroll
+          for (int k = 0; k < 4; ++k) v[k] = T(__longlong_as_double(0x7ff8000000000000ll));
+          atomicOr(&ctl[tl.x].status, 4);
         } else {
-          const long long o = (long long)g.i * ny + g.j;
 #pragma unroll
-          for (int k = 0; k < 4; ++k) v[k] = qin[k * ps + o];
+          for (int k = 0; k < 4; ++k) v[k] = U[k * G::UR * G::UC + sr * G::UC + sc + G::CO];
           if (g.flip2) v[2] = -v[2];
         }
       }
 #pragma unroll
-      for (int k = 0; k < 4; ++k) U[k * G::UR * G::UC + e] = v[k];
+      for (int k = 0; k < 4; ++k) U[k * G::UR * G::UC + r * G::UC + c + G::CO] = v[k];
     }
     __syncthreads();
 
@@ -190,7 +235,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
 #pragma unroll
       for (int s = 0; s < 6; ++s)
 #pragma unroll
-        for (int k = 0; k < 4; ++k) cells[s][k] = U[k * G::UR * G::UC + (fr + s) * G::UC + c + 1];
+        for (int k = 0; k < 4; ++k) cells[s][k] = U[k * G::UR * G::UC + (fr + s) * G::UC + c + 1 + G::CO];
       T ql[4], qr[4];
       pass1_face<T, FAST, false, CHAR>(cells, gamma, ql, qr, weps);
 #pragma unroll
@@ -262,7 +307,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
 #pragma unroll
       for (int s = 0; s < 6; ++s)
 #pragma unroll
-        for (int k = 0; k < 4; ++k) cells[s][k] = U[k * G::UR * G::UC + (r + 1) * G::UC + fc + s];
+        for (int k = 0; k < 4; ++k) cells[s][k] = U[k * G::UR * G::UC + (r + 1) * G::UC + fc + s + G::CO];
       T ql[4], qr[4];
       pass1_face<T, FAST, true, CHAR>(cells, gamma, ql, qr, weps);
 #pragma unroll
@@ -366,13 +411,13 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
         const T dgdy = (fyb - fya) / T(d.dx);
         L[k] = -(dfdx + dgdy);
       }
-      const long long o = (long long)i * ny + j;
+      const long long o = (long long)i * d.ld + j;
       // stage input of this cell, from the tile (padded (i+3, j+3) -> tile (i+3-i0+HF, ...))
       const int ur = i + 3 - i0 + HF, uc = j + 3 - j0 + HF;
       T v[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        const T qs = U[k * G::UR * G::UC + ur * G::UC + uc];
+        const T qs = U[k * G::UR * G::UC + ur * G::UC + uc + G::CO];
         if (stage == 1) {
           v[k] = qs + T(dt) * L[k];
         } else if (stage == 2) {
@@ -403,6 +448,9 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
         if (!(b < INFINITY)) atomicOr(&ctl[tl.x].status, 1);
       }
     }
+    // the next tile's TMA load overwrites U: order this tile's shared-memory
+    // accesses before it
+    tma::fence_proxy_async_smem();
     __syncthreads();
   }
 }
@@ -422,7 +470,7 @@ __global__ void __launch_bounds__(NT) k_cfl_tiles(const SolveDesc* __restrict__ 
     for (int e = tid; e < TX * TY; e += NT) {
       const int i = tl.y + e / TY, j = tl.z + e % TY;
       if (i >= d.nx || j >= d.ny) continue;
-      const long long o = d.off + (long long)i * d.ny + j;
+      const long long o = d.off + (long long)i * d.ld + j;
       const double r0 = (double)Q[o];
       const double rho = fmax(r0, kEps);
       const double uu = (double)Q[o + d.ps] / rho, vv = (double)Q[o + 2 * d.ps] / rho;
@@ -453,6 +501,13 @@ __global__ void k_solve_clock(SolveCtl* ctl, int nsolves, int phase) {
   if (!c.active) return;
   if (phase == 0) {
     const double cmax = __longlong_as_double((long long)c.cmax_bits) + 1e-16;
+    if (!(cmax < INFINITY)) {
+      // a non-finite wave speed (NaN, or an overflow to infinity that would give
+      // dt = 0 for ever): the solve stops here with its status set
+      c.status |= 1;
+      c.active = 0;
+      return;
+    }
     double dt = c.cfl_dx / cmax;
     if (c.t_end >= 0.0) {
       const double remaining = c.t_end - c.t;

@@ -64,11 +64,11 @@ def measure(states, *, precision, mode, cons, force_hlle, jp_cri, cfl, gamma=1.4
     [(q, dx), ...]; configurations that do not fit are reported as None."""
     import torch
     from .batch import Batch
-    cells = sum((q.shape[0] - 6) * (q.shape[1] - 6) for q, _ in states)
+    cells = Batch.pool_cells([(q.shape[0] - 6, q.shape[1] - 6) for q, _ in states], precision)
     times = {}
     for cfg in range(_lib.load().weno_batch_tile_config_count()):
         try:
-            b = Batch(cells + 64 * len(states) + 1024, len(states), precision=precision, mode=mode, cons=cons,
+            b = Batch(cells, len(states), precision=precision, mode=mode, cons=cons,
                       force_hlle=force_hlle, jp_cri=jp_cri, gamma=gamma, cfl=cfl, tile_config=cfg)
         except ValueError:
             times[cfg] = None

@@ -41,6 +41,13 @@ class Batch:
         self.shapes = {}
 
     @staticmethod
+    def pool_cells(shapes, precision=32):
+        """Pool size (cells) that holds solves of the given (nx, ny) shapes at once:
+        rows padded to 16 bytes, each plane rounded up to 64 elements."""
+        q = 16 // (4 if int(precision) == 32 else 8)
+        return sum(((nx * (-(-ny // q) * q) + 63) // 64) * 64 for nx, ny in shapes)
+
+    @staticmethod
     def tile_configs():
         return _lib.load().weno_batch_tile_config_count()
 

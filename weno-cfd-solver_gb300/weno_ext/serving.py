@@ -71,7 +71,9 @@ class Request:
 
 
 def footprint_bytes(nx, ny, precision):
-    return 3 * 4 * (((nx * ny + 63) // 64) * 64) * (4 if precision == 32 else 8)
+    es = 4 if precision == 32 else 8
+    ld = -(-ny // (16 // es)) * (16 // es)  # rows padded to 16 bytes
+    return 3 * 4 * (((nx * ld + 63) // 64) * 64) * es
 
 
 def poisson_stream(n, rate, lo, hi, seed, fp64_fraction=0.25, t_end=(0.1, 0.3), shock_fraction=0.3):
