@@ -332,6 +332,79 @@ def run_c3(args):
     return 0
 
 
+def run_dropin(args):
+    """The reference-facing functions themselves (the weno_ext boundary) at nx x ny:
+    l_local_py on torch CUDA tensors (device-resident) and on numpy arrays (host
+    copies in and out every call), plus the per-direction sweeps it is built from.
+    Unit: cell-residuals/s = interior cells whose L(U) one call evaluates, per second."""
+    import torch
+    torch.cuda.set_device(0)
+    import weno_ext
+    weno_ext.set_mode(args.mode)
+    nx, ny = args.nx, args.ny
+    q = quadrant_state(nx, ny)
+    qd = torch.from_numpy(q).cuda()
+    dx = 1.0 / nx
+    k = max(args.steps, 1)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(k):
+            fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    calls = {
+        "l_local_py char+HLLE": lambda: weno_ext.l_local_py(qd, dx, GAMMA, True, (0.2, 1.0), False),
+        "l_local_py char+blend": lambda: weno_ext.l_local_py(qd, dx, GAMMA, False, (0.2, 1.0), False),
+        "l_local_py cons+HLLE": lambda: weno_ext.l_local_py(qd, dx, GAMMA, True, (0.2, 1.0), True),
+        "weno_x_py": lambda: weno_ext.weno_x_py(qd, GAMMA),
+        "weno_y_py": lambda: weno_ext.weno_y_py(qd, GAMMA),
+        "flux_x_py": lambda: weno_ext.flux_x_py(qd, GAMMA),
+        "con2primi_py": lambda: weno_ext.con2primi_py(qd, GAMMA),
+    }
+    ms = {name: timed(fn) for name, fn in calls.items()}
+    ql, fl, qr, fr = weno_ext.weno_x_py(qd, GAMMA)
+    ms["hlle_x_rs_py"] = timed(lambda: weno_ext.hlle_x_rs_py(ql, fl, qr, fr, GAMMA))
+    ms["hllc_x_rs_py"] = timed(lambda: weno_ext.hllc_x_rs_py(ql, fl, qr, fr, GAMMA))
+    del ql, fl, qr, fr
+    # host arrays: the call copies the input in and the result out (the reference's calling convention)
+    weno_ext.l_local_py(q, dx, GAMMA, True, (0.2, 1.0), False)
+    t0 = time.perf_counter()
+    for _ in range(k):
+        weno_ext.l_local_py(q, dx, GAMMA, True, (0.2, 1.0), False)
+    host_ms = (time.perf_counter() - t0) * 1e3 / k
+    M, N = nx + 6, ny + 6
+    main = ms["l_local_py char+HLLE"]
+    alg = (M * N * 4 + nx * ny * 4) * 8  # stencil input once + residual out once
+    peaks = load_json(os.path.join(ROOT, "MEASURED_PEAKS.json")) or {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    flops = (load_json(os.path.join(ROOT, "profiles", "flops_per_cell.json")) or {}).get("per_residual", {})
+    fpc = flops.get("char_hlle", {}).get("flops")
+    line = {
+        "metric": "cell-residuals/s of l_local_py (char-WENO5+GQ+HLLE, FP64) on device tensors", "config_name": "dropin",
+        "value": nx * ny / (main / 1e3), "unit": "cell-residuals/s", "n_gpus": 1, "dtype": "f64", "data": "synthetic",
+        "higher_is_better": True, "mode": args.mode,
+        "config": {"workload": f"four-quadrant Riemann {nx}x{ny} (+3 ghosts), one residual evaluation per call",
+                   "nx": nx, "ny": ny, "calls_per_measurement": k},
+        "ms_per_call": ms,
+        "host_arrays": {"ms_per_call": host_ms, "value": nx * ny / (host_ms / 1e3), "unit": "cell-residuals/s",
+                        "h2d_bytes": M * N * 8 * 8, "d2h_bytes": nx * ny * 4 * 8},
+        "roofline": {"bound": "hbm", "achieved": alg / (main / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": alg / (main / 1e3) / 1e9 / hbm, "algorithmic_bytes": alg},
+        "compute": ({"achieved_tflops": fpc * nx * ny / (main / 1e3) / 1e12, "flops_per_cell_residual": fpc}
+                    if fpc else None),
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_c4(args):
     """Serving: a seeded Poisson stream of requests (quadrant or oblique-shock initial
     data, FP32 or FP64 tag, seeded t_end) under an HBM budget with continuous batching."""
@@ -392,9 +465,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="headline", choices=["headline", "c1", "c2", "c3", "c4"],
+    ap.add_argument("--config", default="headline", choices=["headline", "c1", "c2", "c3", "c4", "dropin"],
                     help="headline: the 4096^2 FP64 step (default); c1: 2048^2 FP64/FP32 accuracy run; "
-                         "c2: oblique shock 4096x1024 FP32 vs FP64; c3: batched uneven solves; c4: serving stream")
+                         "c2: oblique shock 4096x1024 FP32 vs FP64; c3: batched uneven solves; c4: serving stream; "
+                         "dropin: the weno_ext functions themselves (l_local_py & co.)")
     ap.add_argument("--solves", type=int, default=512)
     ap.add_argument("--requests", type=int, default=300)
     args = ap.parse_args()
@@ -407,6 +481,8 @@ def main():
         return run_c3(args)
     if args.config == "c4":
         return run_c4(args)
+    if args.config == "dropin":
+        return run_dropin(args)
 
     import torch
     from weno_ext import replicas
