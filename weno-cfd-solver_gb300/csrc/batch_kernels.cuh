@@ -119,7 +119,11 @@ struct TileGeom {
   static constexpr int P1_ELEMS = 8 * P1;
   static constexpr int FX_ELEMS = NF * FXR * FXC;
   static constexpr int FY_ELEMS = NF * FYR * FYC;
-  static constexpr int TOTAL = U_ELEMS + P1_ELEMS + FX_ELEMS + FY_ELEMS;
+  // x and y face fluxes share one buffer: the x flux difference of every cell
+  // is kept in DX (4 x TX x TY) before the y sweep overwrites the faces.
+  static constexpr int F_ELEMS = FX_ELEMS > FY_ELEMS ? FX_ELEMS : FY_ELEMS;
+  static constexpr int DX_ELEMS = 4 * TX * TY;
+  static constexpr int TOTAL = U_ELEMS + P1_ELEMS + F_ELEMS + DX_ELEMS;
 };
 
 // Sensor weight at face (fr, fc) of a local face array of R x C entries whose
@@ -158,7 +162,8 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
   T* U = reinterpret_cast<T*>(smem_raw);
   T* P1 = U + G::U_ELEMS;
   T* FX = P1 + G::P1_ELEMS;
-  T* FY = FX + G::FX_ELEMS;
+  T* FY = FX;  // the y faces reuse the x faces' buffer
+  T* DXF = FX + G::F_ELEMS;
   __shared__ double red[NT / 32];
   __shared__ uint64_t bar;
   const int tid = threadIdx.x;
@@ -297,6 +302,32 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
       }
     }
     __syncthreads();
+    // ---- x flux difference of every cell of the tile (sensor blend of the x faces) ----
+    for (int e = tid; e < TX * TY; e += NT) {
+      const int il = e / TY, jl = e % TY;
+      const int i = i0 + il, j = j0 + jl;
+      if (i >= nx || j >= ny) continue;
+      const int fxr = il + HF, fxc = jl + HF;  // Fx rows fi = i, i+1
+      const int FN = G::FXR * G::FXC;
+      T wa = T(1.0), wb = T(1.0);
+      if constexpr (BLEND) {
+        wa = tile_sensor<T, FAST>(FX + 8 * FN, G::FXR, G::FXC, fxr, fxc, i, j, nx + 1, ny, jp_lo, jp_hi);
+        wb = tile_sensor<T, FAST>(FX + 8 * FN, G::FXR, G::FXC, fxr + 1, fxc, i + 1, j, nx + 1, ny, jp_lo, jp_hi);
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        T fxa, fxb;
+        if constexpr (BLEND) {
+          fxa = wa * FX[k * FN + fxr * G::FXC + fxc] + (T(1.0) - wa) * FX[(4 + k) * FN + fxr * G::FXC + fxc];
+          fxb = wb * FX[k * FN + (fxr + 1) * G::FXC + fxc] + (T(1.0) - wb) * FX[(4 + k) * FN + (fxr + 1) * G::FXC + fxc];
+        } else {
+          fxa = FX[k * FN + fxr * G::FXC + fxc];
+          fxb = FX[k * FN + (fxr + 1) * G::FXC + fxc];
+        }
+        DXF[k * TX * TY + e] = (fxb - fxa) / T(d.dx);
+      }
+    }
+    __syncthreads();
 
     // ---- y sweep: pass 1 on rows I = i0+1-HF+r, faces fj = j0-HF+fc ----
     for (int e = tid; e < G::P1YR * G::P1YC; e += NT) {
@@ -382,32 +413,24 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
       const int i = i0 + il, j = j0 + jl;
       if (i >= nx || j >= ny) continue;
       T L[4];
-      const int fxr = il + HF, fxc = jl + HF;  // Fx rows fi = i, i+1
       const int fyr = il + HF, fyc = jl + HF;  // Fy cols fj = j, j+1
+      const int FM = G::FYR * G::FYC;
+      T va = T(1.0), vb = T(1.0);
+      if constexpr (BLEND) {
+        va = tile_sensor<T, FAST>(FY + 8 * FM, G::FYR, G::FYC, fyr, fyc, i, j, nx, ny + 1, jp_lo, jp_hi);
+        vb = tile_sensor<T, FAST>(FY + 8 * FM, G::FYR, G::FYC, fyr, fyc + 1, i, j + 1, nx, ny + 1, jp_lo, jp_hi);
+      }
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        T fxa, fxb, fya, fyb;
+        T fya, fyb;
         if constexpr (BLEND) {
-          const int FN = G::FXR * G::FXC;
-          const T wa = tile_sensor<T, FAST>(FX + 8 * FN, G::FXR, G::FXC, fxr, fxc, i, j, nx + 1, ny, jp_lo, jp_hi);
-          const T wb = tile_sensor<T, FAST>(FX + 8 * FN, G::FXR, G::FXC, fxr + 1, fxc, i + 1, j, nx + 1, ny, jp_lo,
-                                            jp_hi);
-          fxa = wa * FX[k * FN + fxr * G::FXC + fxc] + (T(1.0) - wa) * FX[(4 + k) * FN + fxr * G::FXC + fxc];
-          fxb = wb * FX[k * FN + (fxr + 1) * G::FXC + fxc] + (T(1.0) - wb) * FX[(4 + k) * FN + (fxr + 1) * G::FXC + fxc];
-          const int FM = G::FYR * G::FYC;
-          const T va = tile_sensor<T, FAST>(FY + 8 * FM, G::FYR, G::FYC, fyr, fyc, i, j, nx, ny + 1, jp_lo, jp_hi);
-          const T vb = tile_sensor<T, FAST>(FY + 8 * FM, G::FYR, G::FYC, fyr, fyc + 1, i, j + 1, nx, ny + 1, jp_lo,
-                                            jp_hi);
           fya = va * FY[k * FM + fyr * G::FYC + fyc] + (T(1.0) - va) * FY[(4 + k) * FM + fyr * G::FYC + fyc];
           fyb = vb * FY[k * FM + fyr * G::FYC + fyc + 1] + (T(1.0) - vb) * FY[(4 + k) * FM + fyr * G::FYC + fyc + 1];
         } else {
-          const int FN = G::FXR * G::FXC, FM = G::FYR * G::FYC;
-          fxa = FX[k * FN + fxr * G::FXC + fxc];
-          fxb = FX[k * FN + (fxr + 1) * G::FXC + fxc];
           fya = FY[k * FM + fyr * G::FYC + fyc];
           fyb = FY[k * FM + fyr * G::FYC + fyc + 1];
         }
-        const T dfdx = (fxb - fxa) / T(d.dx);
+        const T dfdx = DXF[k * TX * TY + e];
         const T dgdy = (fyb - fya) / T(d.dx);
         L[k] = -(dfdx + dgdy);
       }
