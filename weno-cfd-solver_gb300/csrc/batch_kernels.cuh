@@ -263,8 +263,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
           const T* p = P1 + k * G::P1 + fr * G::P1XC + fc;
           weno5_gq_pair<T, FAST>(p[0], p[1], p[2], p[3], p[4], a1[k], a2[k], weps);
         }
-        euler_flux<T, FAST, false>(a1, gamma, f1);
-        euler_flux<T, FAST, false>(a2, gamma, f2);
+        euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           fl[k] = T(0.5) * (f1[k] + f2[k]);
@@ -275,8 +274,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
           const T* p = P1 + (4 + k) * G::P1 + fr * G::P1XC + fc;
           weno5_gq_pair<T, FAST>(p[0], p[1], p[2], p[3], p[4], a1[k], a2[k], weps);
         }
-        euler_flux<T, FAST, false>(a1, gamma, f1);
-        euler_flux<T, FAST, false>(a2, gamma, f2);
+        euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           fr_[k] = T(0.5) * (f2[k] + f1[k]);
@@ -324,7 +322,8 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
           fxa = FX[k * FN + fxr * G::FXC + fxc];
           fxb = FX[k * FN + (fxr + 1) * G::FXC + fxc];
         }
-        DXF[k * TX * TY + e] = (fxb - fxa) / T(d.dx);
+        if constexpr (FAST) DXF[k * TX * TY + e] = (fxb - fxa) * qrcp<T, FAST>(T(d.dx));
+        else DXF[k * TX * TY + e] = (fxb - fxa) / T(d.dx);
       }
     }
     __syncthreads();
@@ -362,8 +361,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
           weno5_gq_pair<T, FAST>(p[0], p[G::P1YC], p[2 * G::P1YC], p[3 * G::P1YC], p[4 * G::P1YC], a1[k], a2[k],
                                  weps);
         }
-        euler_flux<T, FAST, true>(a1, gamma, f1);
-        euler_flux<T, FAST, true>(a2, gamma, f2);
+        euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           fl[k] = T(0.5) * (f1[k] + f2[k]);
@@ -375,8 +373,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
           weno5_gq_pair<T, FAST>(p[0], p[G::P1YC], p[2 * G::P1YC], p[3 * G::P1YC], p[4 * G::P1YC], a1[k], a2[k],
                                  weps);
         }
-        euler_flux<T, FAST, true>(a1, gamma, f1);
-        euler_flux<T, FAST, true>(a2, gamma, f2);
+        euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           fr_[k] = T(0.5) * (f2[k] + f1[k]);
@@ -431,7 +428,9 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
           fyb = FY[k * FM + fyr * G::FYC + fyc + 1];
         }
         const T dfdx = DXF[k * TX * TY + e];
-        const T dgdy = (fyb - fya) / T(d.dx);
+        T dgdy;
+        if constexpr (FAST) dgdy = (fyb - fya) * qrcp<T, FAST>(T(d.dx));
+        else dgdy = (fyb - fya) / T(d.dx);
         L[k] = -(dfdx + dgdy);
       }
       const long long o = (long long)i * d.ld + j;

@@ -62,17 +62,27 @@ __device__ __forceinline__ T qrcp(T b) {
   if constexpr (FAST && is_f32<T>) return __fdividef(1.0f, b);
   else return T(1.0) / b;
 }
+// 1/sqrt(x) of the FAST forms (x > 0): one reciprocal square root gives sqrt(x)
+// = x * r and 1/x = r * r, replacing a square root and two divisions.  CUDA's
+// double and float rsqrt (within 1 and 2 ulp); df64 takes 1/sqrt.
+template <class T>
+__device__ __forceinline__ T frsqrt(T x) {
+  if constexpr (is_native_f64<T>) return rsqrt(x);
+  else if constexpr (is_f32<T>) return rsqrtf(x);
+  else return T(1.0) / sqrt(x);
+}
 
 // ---------------------------------------------------------------------------
 // Conserved state helpers (utils.rs:9-35, utils.rs:74-109)
 // ---------------------------------------------------------------------------
-// Euler flux normal to x (Y = false) or y (Y = true), utils.rs:74-109.
+// Euler flux normal to x (Y = false) or y (Y = true), utils.rs:74-109.  `rinv`
+// (FAST only, when > 0) is 1/max(q[0], eps) computed by the caller.
 template <class T, bool FAST, bool Y>
-__device__ __forceinline__ void euler_flux(const T q[4], T gamma, T f[4]) {
+__device__ __forceinline__ void euler_flux(const T q[4], T gamma, T f[4], T rinv = T(0.0)) {
   const T rho = vmax(q[0], T(kEps));
   T u, v;
   if constexpr (FAST) {
-    const T r = qrcp<T, FAST>(rho);
+    const T r = rinv > T(0.0) ? rinv : qrcp<T, FAST>(rho);
     u = q[1] * r;
     v = q[2] * r;
   } else {
@@ -90,6 +100,31 @@ __device__ __forceinline__ void euler_flux(const T q[4], T gamma, T f[4]) {
     f[1] = q[1] * v;
     f[2] = q[2] * v + p;
     f[3] = v * (q[3] + p);
+  }
+}
+
+// Two Euler fluxes (utils.rs:74-109).  FAST native double shares one division
+// between the two densities: 1/(rho_a rho_b), whose product stays in range for
+// any clamped density below 1e150 (otherwise two divisions).
+template <class T, bool FAST, bool Y>
+__device__ __forceinline__ void euler_flux_pair(const T qa[4], const T qb[4], T gamma, T fa[4], T fb[4]) {
+  if constexpr (FAST && is_native_f64<T>) {
+    const T ra = vmax(qa[0], T(kEps)), rb = vmax(qb[0], T(kEps));
+    const T prod = ra * rb;
+    T ia, ib;
+    if (prod < T(1e300)) {
+      const T inv = T(1.0) / prod;
+      ia = rb * inv;
+      ib = ra * inv;
+    } else {
+      ia = T(1.0) / ra;
+      ib = T(1.0) / rb;
+    }
+    euler_flux<T, FAST, Y>(qa, gamma, fa, ia);
+    euler_flux<T, FAST, Y>(qb, gamma, fb, ib);
+  } else {
+    euler_flux<T, FAST, Y>(qa, gamma, fa);
+    euler_flux<T, FAST, Y>(qb, gamma, fb);
   }
 }
 
@@ -148,26 +183,38 @@ __device__ __forceinline__ void js_betas(T u0, T u1, T u2, T u3, T u4, T& b0, T&
   b2 = T(kC13) * (t * t) + T(0.25) * (s * s);
 }
 
-// Power-of-two scale that brings x (> 0, finite) into [0.5, 1): multiplying
-// by it is exact, and its exponent comes from integer operations, so no FP64
-// pipe slot is spent.  Returns 1 for zero, denormal or non-finite x.
-__device__ __forceinline__ double pow2_scale_of(double x) {
-  const int hi = __double2hiint(x);
-  const int e = (hi >> 20) & 0x7ff;  // biased exponent
-  if (e == 0 || e == 0x7ff) return 1.0;
-  // 2^(1022 - e) has biased exponent 2045 - e; clamp to the normal range
-  // (x >= 2^1022 then lands in [0.5, 4), still safe for the products).
-  int b = 2045 - e;
+// Biased exponent of the largest of three positive doubles, from integer
+// operations on the high words (no FP64 slot).
+__device__ __forceinline__ int max_biased_exp3(double a, double b, double c) {
+  const int ea = (__double2hiint(a) >> 20) & 0x7ff;
+  const int eb = (__double2hiint(b) >> 20) & 0x7ff;
+  const int ec = (__double2hiint(c) >> 20) & 0x7ff;
+  return max(ea, max(eb, ec));
+}
+
+// Brings (eps + beta_k) into the range where the fourth-power products of the
+// common-denominator weights neither overflow nor lose the dominant weight.
+// For a largest value within [2^-200, 2^200] (every practical stencil) nothing
+// is done; otherwise all three are scaled by the same power of two that puts
+// the largest into [0.5, 1) (exact).  NaN and infinity pass through.
+__device__ __forceinline__ void weno_range(double& e0, double& e1, double& e2) {
+  const int em = max_biased_exp3(e0, e1, e2);
+  if (em >= 1023 - 200 && em <= 1023 + 200) return;
+  if (em == 0x7ff || em == 0) return;
+  int b = 2045 - em;
   if (b < 1) b = 1;
-  return __hiloint2double(b << 20, 0);
+  const double sc = __hiloint2double(b << 20, 0);
+  e0 *= sc;
+  e1 *= sc;
+  e2 *= sc;
 }
 
 // Non-linear weighting of three candidate values with linear weights d.
 // Exact: the reference's a_k = d_k/(eps+b_k)^2, w_k = a_k/sum.
 // FAST double: one divide via the common denominator prod_j (eps+b_j)^2,
-// with the three (eps+b_k) first scaled by the same power of two so that the
-// largest lies in [0.5, 1) -- the products then neither overflow nor lose the
-// dominant weight, whatever the magnitude of the stencil values.
+// the three (eps+b_k) brought into a safe range first (weno_range) -- the
+// products then neither overflow nor lose the dominant weight, whatever the
+// magnitude of the stencil values.
 // FAST float and df64: reciprocals, because the float exponent range would
 // underflow the products.
 template <class T, bool FAST>
@@ -181,10 +228,7 @@ __device__ __forceinline__ T weno_combine(T e0, T e1, T e2, T d0, T d1, T d2, T 
     const T r = w0 * p0 + w1 * p1 + w2 * p2;
     return scale == T(1.0) ? r : r / scale;
   } else if constexpr (is_native_f64<T>) {
-    const T sc = pow2_scale_of(fmax(fmax(e0, e1), e2));
-    e0 *= sc;
-    e1 *= sc;
-    e2 *= sc;
+    weno_range(e0, e1, e2);
     const T s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
     const T c0 = d0 * (s1 * s2), c1 = d1 * (s0 * s2), c2 = d2 * (s0 * s1);
     const T num = c0 * p0 + c1 * p1 + c2 * p2;
@@ -196,6 +240,33 @@ __device__ __forceinline__ T weno_combine(T e0, T e1, T e2, T d0, T d1, T d2, T 
     const T a2 = d2 * qrcp<T, FAST>(e2 * e2);
     const T num = a0 * p0 + a1 * p1 + a2 * p2;
     return qdiv<T, FAST>(num, (a0 + a1 + a2) * scale);
+  }
+}
+
+// FAST native double: numerator and denominator of weno_combine, so that a
+// caller can share one divide between two reconstructions.
+__device__ __forceinline__ void weno_nd(double e0, double e1, double e2, double d0, double d1, double d2, double p0,
+                                        double p1, double p2, double scale, double& num, double& den) {
+  weno_range(e0, e1, e2);
+  const double s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
+  const double c0 = d0 * (s1 * s2), c1 = d1 * (s0 * s2), c2 = d2 * (s0 * s1);
+  num = c0 * p0 + c1 * p1 + c2 * p2;
+  den = (c0 + c1 + c2) * scale;
+}
+
+// x = a/b and y = c/d with one divide, 1/(b d), when b d is a normal number
+// well inside the double range (tested on its exponent bits, no FP64 slot);
+// otherwise two divides.
+__device__ __forceinline__ void div_pair(double a, double b, double c, double d, double& x, double& y) {
+  const double bd = b * d;
+  const int e = (__double2hiint(bd) >> 20) & 0x7ff;
+  if (e > 64 && e < 1983) {
+    const double inv = 1.0 / bd;
+    x = a * d * inv;
+    y = c * b * inv;
+  } else {
+    x = a / b;
+    y = c / d;
   }
 }
 
@@ -230,6 +301,29 @@ __device__ __forceinline__ T weno5_right(T u1, T u2, T u3, T u4, T u5, T weps) {
   return weno_combine<T, FAST>(weps + b0, weps + b1, weps + b2, T(0.1), T(0.6), T(0.3), p0, p1, p2, T(6.0));
 }
 
+// weno5_left and weno5_right of one field at one face (the right stencil is
+// the left one shifted by a cell), FAST native double with one shared divide.
+__device__ __forceinline__ void weno5_lr_fast(double u0, double u1, double u2, double u3, double u4, double u5,
+                                              double weps, double& left, double& right) {
+  double b0, b1, b2, nl, dl, nr, dr;
+  js_betas(u0, u1, u2, u3, u4, b0, b1, b2);
+  weno_nd(weps + b0, weps + b1, weps + b2, 0.3, 0.6, 0.1, -u4 + 5.0 * u3 + 2.0 * u2, -u1 + 5.0 * u2 + 2.0 * u3,
+          2.0 * u0 - 7.0 * u1 + 11.0 * u2, 6.0, nl, dl);
+  double t, s;
+  t = u3 - 2.0 * u4 + u5;
+  s = 3.0 * u3 - 4.0 * u4 + u5;
+  b0 = kC13 * (t * t) + 0.25 * (s * s);
+  t = u2 - 2.0 * u3 + u4;
+  s = u2 - u4;
+  b1 = kC13 * (t * t) + 0.25 * (s * s);
+  t = u1 - 2.0 * u2 + u3;
+  s = u1 - 4.0 * u2 + 3.0 * u3;
+  b2 = kC13 * (t * t) + 0.25 * (s * s);
+  weno_nd(weps + b0, weps + b1, weps + b2, 0.1, 0.6, 0.3, 2.0 * u5 - 7.0 * u4 + 11.0 * u3, -u4 + 5.0 * u3 + 2.0 * u2,
+          -u1 + 5.0 * u2 + 2.0 * u3, 6.0, nr, dr);
+  div_pair(nl, dl, nr, dr, left, right);
+}
+
 // weno.rs:262-303: both Gauss-point values from one 5-cell stencil.  The
 // smoothness indicators are shared (the reference recomputes identical values).
 template <class T, bool FAST>
@@ -254,8 +348,8 @@ __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& r
     const T pa0 = q2 + g0 * S, pa1 = q2 - g1, pa2 = q2 - g2 * S;
     const T pb0 = q2 - g0 * S, pb1 = q2 + g1, pb2 = q2 + g2 * S;
     if constexpr (is_native_f64<T>) {
-      const T sc = pow2_scale_of(fmax(fmax(e0, e1), e2));
-      const T f0 = e0 * sc, f1 = e1 * sc, f2 = e2 * sc;
+      T f0 = e0, f1 = e1, f2 = e2;
+      weno_range(f0, f1, f2);
       const T s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
       const T P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
       const T ca0 = T(kGqA0) * P0, ca1 = T(kGqA1) * P1, ca2 = T(kGqA2) * P2;
@@ -277,15 +371,39 @@ __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& r
 // Characteristic projection (weno.rs:13-205)
 // ---------------------------------------------------------------------------
 // Roe average of two conserved cells, weno.rs:13-52.
+// FAST also returns 1/c_roe and 1/rho_roe (ic, irho) for the eigenvectors:
+// with r = 1/sqrt(rho) per side, sqrt(rho) = rho r, 1/rho = r r, sqrt(rho) u =
+// m r, and 1/rho_roe = r_l r_r, so the average costs two reciprocal square
+// roots, one divide and one more reciprocal square root for c.
 template <class T, bool FAST>
 __device__ __forceinline__ void roe_avg(const T ul[4], const T ur[4], T gamma, T& rho_roe, T& u_roe, T& v_roe,
-                                        T& h_roe, T& c_roe) {
+                                        T& h_roe, T& c_roe, T& ic, T& irho) {
   const T rho_l = vmax(ul[0], T(kEps));
   const T rho_r = vmax(ur[0], T(kEps));
-  const T sqrt_l = sqrt(rho_l);
-  const T sqrt_r = sqrt(rho_r);
-  const T denom = sqrt_l + sqrt_r;
-  if constexpr (!FAST) {
+  if constexpr (FAST) {
+    const T rl = frsqrt(rho_l), rr = frsqrt(rho_r);
+    const T sqrt_l = rho_l * rl, sqrt_r = rho_r * rr;
+    const T il = rl * rl, ir = rr * rr;
+    const T u_l = ul[1] * il, v_l = ul[2] * il;
+    const T u_r = ur[1] * ir, v_r = ur[2] * ir;
+    const T p_l = vmax((gamma - T(1.0)) * (ul[3] - T(0.5) * rho_l * (u_l * u_l + v_l * v_l)), T(kEps));
+    const T p_r = vmax((gamma - T(1.0)) * (ur[3] - T(0.5) * rho_r * (u_r * u_r + v_r * v_r)), T(kEps));
+    const T id = qrcp<T, FAST>(sqrt_l + sqrt_r);
+    u_roe = (ul[1] * rl + ur[1] * rr) * id;
+    v_roe = (ul[2] * rl + ur[2] * rr) * id;
+    h_roe = ((ul[3] + p_l) * rl + (ur[3] + p_r) * rr) * id;
+    const T kin = T(0.5) * (u_roe * u_roe + v_roe * v_roe);
+    const T c2 = vmax((gamma - T(1.0)) * (h_roe - kin), T(kEps) * vmax(il, ir));
+    ic = frsqrt(c2);
+    c_roe = c2 * ic;
+    rho_roe = sqrt_l * sqrt_r;
+    irho = rl * rr;
+  } else {
+    (void)ic;
+    (void)irho;
+    const T sqrt_l = sqrt(rho_l);
+    const T sqrt_r = sqrt(rho_r);
+    const T denom = sqrt_l + sqrt_r;
     const T u_l = ul[1] / rho_l, v_l = ul[2] / rho_l;
     const T u_r = ur[1] / rho_r, v_r = ur[2] / rho_r;
     const T p_l = vmax((gamma - T(1.0)) * (ul[3] - T(0.5) * rho_l * (u_l * u_l + v_l * v_l)), T(kEps));
@@ -295,30 +413,16 @@ __device__ __forceinline__ void roe_avg(const T ul[4], const T ur[4], T gamma, T
     u_roe = (sqrt_l * u_l + sqrt_r * u_r) / denom;
     v_roe = (sqrt_l * v_l + sqrt_r * v_r) / denom;
     h_roe = (sqrt_l * h_l + sqrt_r * h_r) / denom;
-  } else {
-    const T il = qrcp<T, FAST>(rho_l), ir = qrcp<T, FAST>(rho_r);
-    const T u_l = ul[1] * il, v_l = ul[2] * il;
-    const T u_r = ur[1] * ir, v_r = ur[2] * ir;
-    const T p_l = vmax((gamma - T(1.0)) * (ul[3] - T(0.5) * rho_l * (u_l * u_l + v_l * v_l)), T(kEps));
-    const T p_r = vmax((gamma - T(1.0)) * (ur[3] - T(0.5) * rho_r * (u_r * u_r + v_r * v_r)), T(kEps));
-    const T h_l = (ul[3] + p_l) * il;
-    const T h_r = (ur[3] + p_r) * ir;
-    const T id = qrcp<T, FAST>(denom);
-    u_roe = (sqrt_l * u_l + sqrt_r * u_r) * id;
-    v_roe = (sqrt_l * v_l + sqrt_r * v_r) * id;
-    h_roe = (sqrt_l * h_l + sqrt_r * h_r) * id;
+    const T kin = T(0.5) * (u_roe * u_roe + v_roe * v_roe);
+    const T c2 = vmax((gamma - T(1.0)) * (h_roe - kin), T(kEps) / vmin(rho_l, rho_r));
+    c_roe = sqrt(c2);
+    rho_roe = sqrt_l * sqrt_r;
   }
-  const T kin = T(0.5) * (u_roe * u_roe + v_roe * v_roe);
-  T c2;
-  if constexpr (!FAST) c2 = vmax((gamma - T(1.0)) * (h_roe - kin), T(kEps) / vmin(rho_l, rho_r));
-  else c2 = vmax((gamma - T(1.0)) * (h_roe - kin), T(kEps) * vmax(qrcp<T, FAST>(rho_l), qrcp<T, FAST>(rho_r)));
-  c_roe = sqrt(c2);
-  rho_roe = sqrt_l * sqrt_r;
 }
 
 // Left eigenvectors, weno.rs:76-107 (x) and weno.rs:136-167 (y).
 template <class T, bool FAST, bool Y>
-__device__ __forceinline__ void left_eig(T rho, T u, T v, T c, T gamma, T L[4][4]) {
+__device__ __forceinline__ void left_eig(T rho, T u, T v, T c, T gamma, T L[4][4], T ic_in, T irho_in) {
   const T g1 = gamma - T(1.0);
   const T kin = T(0.5) * (u * u + v * v);
   T inv_rc, inv_c2, a, b, irho;
@@ -330,8 +434,8 @@ __device__ __forceinline__ void left_eig(T rho, T u, T v, T c, T gamma, T L[4][4
     a = g1 * kin / (T(2.0) * c * c);
     b = vn / (T(2.0) * c);
   } else {
-    const T ic = qrcp<T, FAST>(c);
-    irho = qrcp<T, FAST>(rho);
+    const T ic = ic_in;
+    irho = irho_in;
     inv_rc = ic * irho;
     inv_c2 = ic * ic;
     a = T(0.5) * (g1 * kin) * inv_c2;
@@ -413,6 +517,13 @@ __device__ __forceinline__ void pp_limit(T q[4], const T ub[4], T gamma) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) q[k] = theta * (q[k] - ub[k]) + ub[k];
   }
+  if constexpr (FAST) {
+    // p < eps  <=>  (gamma-1)(E rho - |m|^2/2) < eps rho for rho > 0 (pp_pressure
+    // is 0 for rho <= 0): the divide is only needed when the limiter acts.
+    if (q[0] > T(0.0) &&
+        !((gamma - T(1.0)) * (q[3] * q[0] - T(0.5) * (q[1] * q[1] + q[2] * q[2])) < T(kEps) * q[0]))
+      return;
+  }
   const T p_q = pp_pressure<T, FAST>(q, gamma);
   if (p_q < T(kEps)) {
     const T p_bar = vmax(pp_pressure<T, FAST>(ub, gamma), T(kEps));
@@ -432,14 +543,18 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
   if constexpr (!CHAR) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      ql[k] = weno5_left<T, FAST>(c[0][k], c[1][k], c[2][k], c[3][k], c[4][k], weps);
-      qr[k] = weno5_right<T, FAST>(c[1][k], c[2][k], c[3][k], c[4][k], c[5][k], weps);
+      if constexpr (FAST && is_native_f64<T>) {
+        weno5_lr_fast(c[0][k], c[1][k], c[2][k], c[3][k], c[4][k], c[5][k], weps, ql[k], qr[k]);
+      } else {
+        ql[k] = weno5_left<T, FAST>(c[0][k], c[1][k], c[2][k], c[3][k], c[4][k], weps);
+        qr[k] = weno5_right<T, FAST>(c[1][k], c[2][k], c[3][k], c[4][k], c[5][k], weps);
+      }
     }
   } else {
-    T rho_a, u_a, v_a, h_a, c_a;
-    roe_avg<T, FAST>(c[2], c[3], gamma, rho_a, u_a, v_a, h_a, c_a);
+    T rho_a, u_a, v_a, h_a, c_a, ic_a = T(0.0), irho_a = T(0.0);
+    roe_avg<T, FAST>(c[2], c[3], gamma, rho_a, u_a, v_a, h_a, c_a, ic_a, irho_a);
     T Lm[4][4];
-    left_eig<T, FAST, Y>(rho_a, u_a, v_a, c_a, gamma, Lm);
+    left_eig<T, FAST, Y>(rho_a, u_a, v_a, c_a, gamma, Lm, ic_a, irho_a);
     // The reference projects cells 0..4 for the left state and 1..5 for the
     // right state with the same matrix (both faces use the Roe average of
     // cells 2|3), so six projections cover both.
@@ -449,8 +564,12 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
     T chl[4], chr[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      chl[k] = weno5_left<T, FAST>(w[0][k], w[1][k], w[2][k], w[3][k], w[4][k], weps);
-      chr[k] = weno5_right<T, FAST>(w[1][k], w[2][k], w[3][k], w[4][k], w[5][k], weps);
+      if constexpr (FAST && is_native_f64<T>) {
+        weno5_lr_fast(w[0][k], w[1][k], w[2][k], w[3][k], w[4][k], w[5][k], weps, chl[k], chr[k]);
+      } else {
+        chl[k] = weno5_left<T, FAST>(w[0][k], w[1][k], w[2][k], w[3][k], w[4][k], weps);
+        chr[k] = weno5_right<T, FAST>(w[1][k], w[2][k], w[3][k], w[4][k], w[5][k], weps);
+      }
     }
     T Rm[4][4];
     right_eig<T, Y>(rho_a, u_a, v_a, h_a, c_a, Rm);
@@ -476,11 +595,14 @@ __device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], con
   r.ql0 = vmax(ql[0], T(kEps));
   r.qr0 = vmax(qr[0], T(kEps));
   T h_l, h_r, u_t, v_t, h_t;
+  T rsl = T(0.0), rsr = T(0.0);  // FAST: 1/sqrt(rho) per side
   if constexpr (!FAST) {
     r.u_l = ql[1] / r.ql0; r.v_l = ql[2] / r.ql0;
     r.u_r = qr[1] / r.qr0; r.v_r = qr[2] / r.qr0;
   } else {
-    const T il = qrcp<T, FAST>(r.ql0), ir = qrcp<T, FAST>(r.qr0);
+    rsl = frsqrt(r.ql0);
+    rsr = frsqrt(r.qr0);
+    const T il = rsl * rsl, ir = rsr * rsr;
     r.u_l = ql[1] * il; r.v_l = ql[2] * il;
     r.u_r = qr[1] * ir; r.v_r = qr[2] * ir;
   }
@@ -489,21 +611,20 @@ __device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], con
   r.p_r = (gamma - T(1.0)) * (qr[3] - T(0.5) * r.qr0 * (r.u_r * r.u_r + r.v_r * r.v_r));
   r.p_l = vmax(r.p_l, T(kEps));
   r.p_r = vmax(r.p_r, T(kEps));
-  const T srl = sqrt(r.ql0), srr = sqrt(r.qr0);
-  const T denom_r = srl + srr;
   if constexpr (!FAST) {
+    const T srl = sqrt(r.ql0), srr = sqrt(r.qr0);
+    const T denom_r = srl + srr;
     h_l = (ql[3] + r.p_l) / r.ql0;
     h_r = (qr[3] + r.p_r) / r.qr0;
     u_t = (srl * r.u_l + srr * r.u_r) / denom_r;
     v_t = (srl * r.v_l + srr * r.v_r) / denom_r;
     h_t = (srl * h_l + srr * h_r) / denom_r;
   } else {
-    // sqrt(rho)*h = (E+p)/sqrt(rho): one reciprocal square root per side.
-    const T il = qrcp<T, FAST>(srl), ir = qrcp<T, FAST>(srr);
-    const T id = qrcp<T, FAST>(denom_r);
-    u_t = (ql[1] * il + qr[1] * ir) * id;
-    v_t = (ql[2] * il + qr[2] * ir) * id;
-    h_t = ((ql[3] + r.p_l) * il + (qr[3] + r.p_r) * ir) * id;
+    // sqrt(rho) = rho r and sqrt(rho)*h = (E+p) r with r = 1/sqrt(rho) per side.
+    const T id = qrcp<T, FAST>(r.ql0 * rsl + r.qr0 * rsr);
+    u_t = (ql[1] * rsl + qr[1] * rsr) * id;
+    v_t = (ql[2] * rsl + qr[2] * rsr) * id;
+    h_t = ((ql[3] + r.p_l) * rsl + (qr[3] + r.p_r) * rsr) * id;
   }
   const T tmp = h_t - T(0.5) * (u_t * u_t + v_t * v_t);
   const T a_t = sqrt(vmax((gamma - T(1.0)) * tmp, T(0.0)));

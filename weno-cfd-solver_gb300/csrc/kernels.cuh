@@ -127,16 +127,14 @@ __global__ void __launch_bounds__(128) k_pass2(Planes<T> PL, Planes<T> PR, int64
   {
     T a1[4], a2[4], f1[4], f2[4];
     gq_face<T, FAST, Y>(PL, row, col, a1, a2, weps);
-    euler_flux<T, FAST, Y>(a1, gamma, f1);
-    euler_flux<T, FAST, Y>(a2, gamma, f2);
+    euler_flux_pair<T, FAST, Y>(a1, a2, gamma, f1, f2);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       fl[k] = T(0.5) * (f1[k] + f2[k]);
       ql[k] = T(0.5) * (a1[k] + a2[k]);
     }
     gq_face<T, FAST, Y>(PR, row, col, a1, a2, weps);
-    euler_flux<T, FAST, Y>(a1, gamma, f1);
-    euler_flux<T, FAST, Y>(a2, gamma, f2);
+    euler_flux_pair<T, FAST, Y>(a1, a2, gamma, f1, f2);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       fr[k] = T(0.5) * (f2[k] + f1[k]);
@@ -256,7 +254,7 @@ __global__ void __launch_bounds__(128) k_blend(Planes<T> Fc, Planes<T> Fe, Plane
 // Fx planes are (m-5) x (n-6) faces, Fy planes (m-6) x (n-5).
 // ---------------------------------------------------------------------------
 
-template <class T, int STAGE>
+template <class T, bool FAST, int STAGE>
 __global__ void __launch_bounds__(128) k_residual(Planes<T> Fx, Planes<T> Fy, int64_t rows, int64_t cols, T dx,
                                                    T* out, Planes<T> Qn, Planes<T> Qs, Planes<T> Qo,
                                                    const StepCtl* ctl) {
@@ -267,11 +265,20 @@ __global__ void __launch_bounds__(128) k_residual(Planes<T> Fx, Planes<T> Fy, in
     if (!ctl->active) return;
   }
   T L[4];
+  if constexpr (FAST) {
+    // one reciprocal instead of eight divides (riemann.rs:527 divides both
+    // differences by the same dx)
+    const T idx = qrcp<T, FAST>(dx);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const T dfdx = (Fx.at(k, row + 1, col) - Fx.at(k, row, col)) / dx;
-    const T dgdy = (Fy.at(k, row, col + 1) - Fy.at(k, row, col)) / dx;
-    L[k] = -(dfdx + dgdy);
+    for (int k = 0; k < 4; ++k)
+      L[k] = -((Fx.at(k, row + 1, col) - Fx.at(k, row, col)) + (Fy.at(k, row, col + 1) - Fy.at(k, row, col))) * idx;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const T dfdx = (Fx.at(k, row + 1, col) - Fx.at(k, row, col)) / dx;
+      const T dgdy = (Fy.at(k, row, col + 1) - Fy.at(k, row, col)) / dx;
+      L[k] = -(dfdx + dgdy);
+    }
   }
   if constexpr (STAGE == 0) {
 #pragma unroll

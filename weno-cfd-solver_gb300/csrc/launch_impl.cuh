@@ -119,10 +119,10 @@ cudaError_t Launch<T, FAST>::residual(HostPlanes Fx, HostPlanes Fy, int64_t rows
   auto X = planes<T>(Fx), Yp = planes<T>(Fy), N = planes<T>(Qn), S = planes<T>(Qs), O = planes<T>(Qo);
   T* o = static_cast<T*>(out);
   switch (stage) {
-    case 0: k_residual<T, 0><<<g, kBlk, 0, st>>>(X, Yp, rows, cols, (T)dx, o, N, S, O, ctl); break;
-    case 1: k_residual<T, 1><<<g, kBlk, 0, st>>>(X, Yp, rows, cols, (T)dx, o, N, S, O, ctl); break;
-    case 2: k_residual<T, 2><<<g, kBlk, 0, st>>>(X, Yp, rows, cols, (T)dx, o, N, S, O, ctl); break;
-    default: k_residual<T, 3><<<g, kBlk, 0, st>>>(X, Yp, rows, cols, (T)dx, o, N, S, O, ctl); break;
+    case 0: k_residual<T, FAST, 0><<<g, kBlk, 0, st>>>(X, Yp, rows, cols, (T)dx, o, N, S, O, ctl); break;
+    case 1: k_residual<T, FAST, 1><<<g, kBlk, 0, st>>>(X, Yp, rows, cols, (T)dx, o, N, S, O, ctl); break;
+    case 2: k_residual<T, FAST, 2><<<g, kBlk, 0, st>>>(X, Yp, rows, cols, (T)dx, o, N, S, O, ctl); break;
+    default: k_residual<T, FAST, 3><<<g, kBlk, 0, st>>>(X, Yp, rows, cols, (T)dx, o, N, S, O, ctl); break;
   }
   return cudaGetLastError();
 }
