@@ -305,22 +305,24 @@ __device__ __forceinline__ T weno5_right(T u1, T u2, T u3, T u4, T u5, T weps) {
 // the left one shifted by a cell), FAST native double with one shared divide.
 __device__ __forceinline__ void weno5_lr_fast(double u0, double u1, double u2, double u3, double u4, double u5,
                                               double weps, double& left, double& right) {
-  double b0, b1, b2, nl, dl, nr, dr;
-  js_betas(u0, u1, u2, u3, u4, b0, b1, b2);
-  weno_nd(weps + b0, weps + b1, weps + b2, 0.3, 0.6, 0.1, -u4 + 5.0 * u3 + 2.0 * u2, -u1 + 5.0 * u2 + 2.0 * u3,
-          2.0 * u0 - 7.0 * u1 + 11.0 * u2, 6.0, nl, dl);
-  double t, s;
-  t = u3 - 2.0 * u4 + u5;
-  s = 3.0 * u3 - 4.0 * u4 + u5;
-  b0 = kC13 * (t * t) + 0.25 * (s * s);
-  t = u2 - 2.0 * u3 + u4;
-  s = u2 - u4;
-  b1 = kC13 * (t * t) + 0.25 * (s * s);
-  t = u1 - 2.0 * u2 + u3;
-  s = u1 - 4.0 * u2 + 3.0 * u3;
-  b2 = kC13 * (t * t) + 0.25 * (s * s);
-  weno_nd(weps + b0, weps + b1, weps + b2, 0.1, 0.6, 0.3, 2.0 * u5 - 7.0 * u4 + 11.0 * u3, -u4 + 5.0 * u3 + 2.0 * u2,
-          -u1 + 5.0 * u2 + 2.0 * u3, 6.0, nr, dr);
+  // first differences d_m = u_{m+1} - u_m, second differences D_m = d_m - d_{m-1}
+  // (centred on u_m), shared by the two stencils; each Jiang-Shu indicator is
+  // 13/12 D^2 + 1/4 s^2 with s a combination of two first differences.
+  const double d0 = u1 - u0, d1 = u2 - u1, d2 = u3 - u2, d3 = u4 - u3, d4 = u5 - u4;
+  const double D1 = d1 - d0, D2 = d2 - d1, D3 = d3 - d2, D4 = d4 - d3;
+  const double C1 = kC13 * (D1 * D1), C2 = kC13 * (D2 * D2), C3 = kC13 * (D3 * D3), C4 = kC13 * (D4 * D4);
+  double sl0 = d3 - 3.0 * d2, sl1 = d1 + d2, sl2 = 3.0 * d1 - d0;   // left:  stencils 2-4, 1-3, 0-2
+  double sr0 = d4 - 3.0 * d3, sr1 = d2 + d3, sr2 = 3.0 * d2 - d1;   // right: stencils 3-5, 2-4, 1-3
+  const double el0 = weps + (C3 + 0.25 * (sl0 * sl0)), el1 = weps + (C2 + 0.25 * (sl1 * sl1)),
+               el2 = weps + (C1 + 0.25 * (sl2 * sl2));
+  const double er0 = weps + (C4 + 0.25 * (sr0 * sr0)), er1 = weps + (C3 + 0.25 * (sr1 * sr1)),
+               er2 = weps + (C2 + 0.25 * (sr2 * sr2));
+  // candidate polynomials (x6): the right stencil's p1, p2 are the left's p0, p1
+  const double pl0 = -u4 + 5.0 * u3 + 2.0 * u2, pl1 = -u1 + 5.0 * u2 + 2.0 * u3;
+  const double pl2 = 2.0 * u0 - 7.0 * u1 + 11.0 * u2, pr0 = 2.0 * u5 - 7.0 * u4 + 11.0 * u3;
+  double nl, dl, nr, dr;
+  weno_nd(el0, el1, el2, 0.3, 0.6, 0.1, pl0, pl1, pl2, 6.0, nl, dl);
+  weno_nd(er0, er1, er2, 0.1, 0.6, 0.3, pr0, pl0, pl1, 6.0, nr, dr);
   div_pair(nl, dl, nr, dr, left, right);
 }
 
@@ -328,10 +330,34 @@ __device__ __forceinline__ void weno5_lr_fast(double u0, double u1, double u2, d
 // smoothness indicators are shared (the reference recomputes identical values).
 template <class T, bool FAST>
 __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& ra, T& rb, T weps) {
+  const T S = T(kSqrt3_12);
+  if constexpr (FAST && is_native_f64<T>) {
+    // difference form (as in weno5_lr_fast): the one-sided indicator terms are
+    // the polynomial slopes g0, g2 and the centred one is g1/S
+    const T d0 = q1 - q0, d1 = q2 - q1, d2 = q3 - q2, d3 = q4 - q3;
+    const T D1 = d1 - d0, D2 = d2 - d1, D3 = d3 - d2;
+    const T h0 = d3 - T(3.0) * d2;  // 3 q2 - 4 q3 + q4
+    const T h1 = d1 + d2;           // q3 - q1
+    const T h2 = T(3.0) * d1 - d0;  // 3 q2 - 4 q1 + q0
+    T f0 = weps + (T(kC13) * (D3 * D3) + T(0.25) * (h0 * h0));
+    T f1 = weps + (T(kC13) * (D2 * D2) + T(0.25) * (h1 * h1));
+    T f2 = weps + (T(kC13) * (D1 * D1) + T(0.25) * (h2 * h2));
+    const T a0 = h0 * S, a1 = h1 * S, a2 = h2 * S;
+    const T pa0 = q2 + a0, pa1 = q2 - a1, pa2 = q2 - a2;
+    const T pb0 = q2 - a0, pb1 = q2 + a1, pb2 = q2 + a2;
+    weno_range(f0, f1, f2);
+    const T s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
+    const T P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
+    const T ca0 = T(kGqA0) * P0, ca1 = T(kGqA1) * P1, ca2 = T(kGqA2) * P2;
+    const T cb0 = T(kGqA2) * P0, cb2 = T(kGqA0) * P2;
+    const T inv = T(1.0) / ((ca0 + ca1 + ca2) * (cb0 + ca1 + cb2));
+    ra = (ca0 * pa0 + ca1 * pa1 + ca2 * pa2) * (cb0 + ca1 + cb2) * inv;
+    rb = (cb0 * pb0 + ca1 * pb1 + cb2 * pb2) * (ca0 + ca1 + ca2) * inv;
+    return;
+  }
   T b0, b1, b2;
   js_betas(q0, q1, q2, q3, q4, b0, b1, b2);
   const T e0 = weps + b0, e1 = weps + b1, e2 = weps + b2;
-  const T S = T(kSqrt3_12);
   const T g0 = T(3.0) * q2 - T(4.0) * q3 + q4;
   const T g2 = T(3.0) * q2 - T(4.0) * q1 + q0;
   if constexpr (!FAST) {
@@ -344,26 +370,15 @@ __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& r
     const T pb2 = q2 + g2 * S;
     rb = weno_combine<T, FAST>(e0, e1, e2, T(kGqA2), T(kGqA1), T(kGqA0), pb0, pb1, pb2, T(1.0));
   } else {
+    // float and df64: reciprocal form
     const T g1 = (q3 - q1) * S;
     const T pa0 = q2 + g0 * S, pa1 = q2 - g1, pa2 = q2 - g2 * S;
     const T pb0 = q2 - g0 * S, pb1 = q2 + g1, pb2 = q2 + g2 * S;
-    if constexpr (is_native_f64<T>) {
-      T f0 = e0, f1 = e1, f2 = e2;
-      weno_range(f0, f1, f2);
-      const T s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
-      const T P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
-      const T ca0 = T(kGqA0) * P0, ca1 = T(kGqA1) * P1, ca2 = T(kGqA2) * P2;
-      const T cb0 = T(kGqA2) * P0, cb2 = T(kGqA0) * P2;
-      const T inv = T(1.0) / ((ca0 + ca1 + ca2) * (cb0 + ca1 + cb2));
-      ra = (ca0 * pa0 + ca1 * pa1 + ca2 * pa2) * (cb0 + ca1 + cb2) * inv;
-      rb = (cb0 * pb0 + ca1 * pb1 + cb2 * pb2) * (ca0 + ca1 + ca2) * inv;
-    } else {
-      const T r0 = qrcp<T, FAST>(e0 * e0), r1 = qrcp<T, FAST>(e1 * e1), r2 = qrcp<T, FAST>(e2 * e2);
-      const T ca0 = T(kGqA0) * r0, ca1 = T(kGqA1) * r1, ca2 = T(kGqA2) * r2;
-      const T cb0 = T(kGqA2) * r0, cb2 = T(kGqA0) * r2;
-      ra = qdiv<T, FAST>(ca0 * pa0 + ca1 * pa1 + ca2 * pa2, ca0 + ca1 + ca2);
-      rb = qdiv<T, FAST>(cb0 * pb0 + ca1 * pb1 + cb2 * pb2, cb0 + ca1 + cb2);
-    }
+    const T r0 = qrcp<T, FAST>(e0 * e0), r1 = qrcp<T, FAST>(e1 * e1), r2 = qrcp<T, FAST>(e2 * e2);
+    const T ca0 = T(kGqA0) * r0, ca1 = T(kGqA1) * r1, ca2 = T(kGqA2) * r2;
+    const T cb0 = T(kGqA2) * r0, cb2 = T(kGqA0) * r2;
+    ra = qdiv<T, FAST>(ca0 * pa0 + ca1 * pa1 + ca2 * pa2, ca0 + ca1 + ca2);
+    rb = qdiv<T, FAST>(cb0 * pb0 + ca1 * pb1 + cb2 * pb2, cb0 + ca1 + cb2);
   }
 }
 
