@@ -303,27 +303,32 @@ __device__ __forceinline__ T weno5_right(T u1, T u2, T u3, T u4, T u5, T weps) {
 
 // weno5_left and weno5_right of one field at one face (the right stencil is
 // the left one shifted by a cell), FAST native double with one shared divide.
-__device__ __forceinline__ void weno5_lr_fast(double u0, double u1, double u2, double u3, double u4, double u5,
-                                              double weps, double& left, double& right) {
+template <class T>
+__device__ __forceinline__ void weno5_lr_fast(T u0, T u1, T u2, T u3, T u4, T u5, T weps, T& left, T& right) {
   // first differences d_m = u_{m+1} - u_m, second differences D_m = d_m - d_{m-1}
   // (centred on u_m), shared by the two stencils; each Jiang-Shu indicator is
   // 13/12 D^2 + 1/4 s^2 with s a combination of two first differences.
-  const double d0 = u1 - u0, d1 = u2 - u1, d2 = u3 - u2, d3 = u4 - u3, d4 = u5 - u4;
-  const double D1 = d1 - d0, D2 = d2 - d1, D3 = d3 - d2, D4 = d4 - d3;
-  const double C1 = kC13 * (D1 * D1), C2 = kC13 * (D2 * D2), C3 = kC13 * (D3 * D3), C4 = kC13 * (D4 * D4);
-  double sl0 = d3 - 3.0 * d2, sl1 = d1 + d2, sl2 = 3.0 * d1 - d0;   // left:  stencils 2-4, 1-3, 0-2
-  double sr0 = d4 - 3.0 * d3, sr1 = d2 + d3, sr2 = 3.0 * d2 - d1;   // right: stencils 3-5, 2-4, 1-3
-  const double el0 = weps + (C3 + 0.25 * (sl0 * sl0)), el1 = weps + (C2 + 0.25 * (sl1 * sl1)),
-               el2 = weps + (C1 + 0.25 * (sl2 * sl2));
-  const double er0 = weps + (C4 + 0.25 * (sr0 * sr0)), er1 = weps + (C3 + 0.25 * (sr1 * sr1)),
-               er2 = weps + (C2 + 0.25 * (sr2 * sr2));
+  const T d0 = u1 - u0, d1 = u2 - u1, d2 = u3 - u2, d3 = u4 - u3, d4 = u5 - u4;
+  const T D1 = d1 - d0, D2 = d2 - d1, D3 = d3 - d2, D4 = d4 - d3;
+  const T C1 = T(kC13) * (D1 * D1), C2 = T(kC13) * (D2 * D2), C3 = T(kC13) * (D3 * D3), C4 = T(kC13) * (D4 * D4);
+  const T sl0 = d3 - T(3.0) * d2, sl1 = d1 + d2, sl2 = T(3.0) * d1 - d0;  // left:  stencils 2-4, 1-3, 0-2
+  const T sr0 = d4 - T(3.0) * d3, sr1 = d2 + d3, sr2 = T(3.0) * d2 - d1;  // right: stencils 3-5, 2-4, 1-3
+  const T el0 = weps + (C3 + T(0.25) * (sl0 * sl0)), el1 = weps + (C2 + T(0.25) * (sl1 * sl1)),
+          el2 = weps + (C1 + T(0.25) * (sl2 * sl2));
+  const T er0 = weps + (C4 + T(0.25) * (sr0 * sr0)), er1 = weps + (C3 + T(0.25) * (sr1 * sr1)),
+          er2 = weps + (C2 + T(0.25) * (sr2 * sr2));
   // candidate polynomials (x6): the right stencil's p1, p2 are the left's p0, p1
-  const double pl0 = -u4 + 5.0 * u3 + 2.0 * u2, pl1 = -u1 + 5.0 * u2 + 2.0 * u3;
-  const double pl2 = 2.0 * u0 - 7.0 * u1 + 11.0 * u2, pr0 = 2.0 * u5 - 7.0 * u4 + 11.0 * u3;
-  double nl, dl, nr, dr;
-  weno_nd(el0, el1, el2, 0.3, 0.6, 0.1, pl0, pl1, pl2, 6.0, nl, dl);
-  weno_nd(er0, er1, er2, 0.1, 0.6, 0.3, pr0, pl0, pl1, 6.0, nr, dr);
-  div_pair(nl, dl, nr, dr, left, right);
+  const T pl0 = -u4 + T(5.0) * u3 + T(2.0) * u2, pl1 = -u1 + T(5.0) * u2 + T(2.0) * u3;
+  const T pl2 = T(2.0) * u0 - T(7.0) * u1 + T(11.0) * u2, pr0 = T(2.0) * u5 - T(7.0) * u4 + T(11.0) * u3;
+  if constexpr (is_native_f64<T>) {
+    double nl, dl, nr, dr;
+    weno_nd(el0, el1, el2, 0.3, 0.6, 0.1, pl0, pl1, pl2, 6.0, nl, dl);
+    weno_nd(er0, er1, er2, 0.1, 0.6, 0.3, pr0, pl0, pl1, 6.0, nr, dr);
+    div_pair(nl, dl, nr, dr, left, right);
+  } else {
+    left = weno_combine<T, true>(el0, el1, el2, T(0.3), T(0.6), T(0.1), pl0, pl1, pl2, T(6.0));
+    right = weno_combine<T, true>(er0, er1, er2, T(0.1), T(0.6), T(0.3), pr0, pl0, pl1, T(6.0));
+  }
 }
 
 // weno.rs:262-303: both Gauss-point values from one 5-cell stencil.  The
@@ -331,7 +336,7 @@ __device__ __forceinline__ void weno5_lr_fast(double u0, double u1, double u2, d
 template <class T, bool FAST>
 __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& ra, T& rb, T weps) {
   const T S = T(kSqrt3_12);
-  if constexpr (FAST && is_native_f64<T>) {
+  if constexpr (FAST) {
     // difference form (as in weno5_lr_fast): the one-sided indicator terms are
     // the polynomial slopes g0, g2 and the centred one is g1/S
     const T d0 = q1 - q0, d1 = q2 - q1, d2 = q3 - q2, d3 = q4 - q3;
@@ -345,22 +350,29 @@ __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& r
     const T a0 = h0 * S, a1 = h1 * S, a2 = h2 * S;
     const T pa0 = q2 + a0, pa1 = q2 - a1, pa2 = q2 - a2;
     const T pb0 = q2 - a0, pb1 = q2 + a1, pb2 = q2 + a2;
-    weno_range(f0, f1, f2);
-    const T s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
-    const T P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
-    const T ca0 = T(kGqA0) * P0, ca1 = T(kGqA1) * P1, ca2 = T(kGqA2) * P2;
-    const T cb0 = T(kGqA2) * P0, cb2 = T(kGqA0) * P2;
-    const T inv = T(1.0) / ((ca0 + ca1 + ca2) * (cb0 + ca1 + cb2));
-    ra = (ca0 * pa0 + ca1 * pa1 + ca2 * pa2) * (cb0 + ca1 + cb2) * inv;
-    rb = (cb0 * pb0 + ca1 * pb1 + cb2 * pb2) * (ca0 + ca1 + ca2) * inv;
-    return;
-  }
-  T b0, b1, b2;
-  js_betas(q0, q1, q2, q3, q4, b0, b1, b2);
-  const T e0 = weps + b0, e1 = weps + b1, e2 = weps + b2;
-  const T g0 = T(3.0) * q2 - T(4.0) * q3 + q4;
-  const T g2 = T(3.0) * q2 - T(4.0) * q1 + q0;
-  if constexpr (!FAST) {
+    if constexpr (is_native_f64<T>) {
+      weno_range(f0, f1, f2);
+      const T s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
+      const T P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
+      const T ca0 = T(kGqA0) * P0, ca1 = T(kGqA1) * P1, ca2 = T(kGqA2) * P2;
+      const T cb0 = T(kGqA2) * P0, cb2 = T(kGqA0) * P2;
+      const T inv = T(1.0) / ((ca0 + ca1 + ca2) * (cb0 + ca1 + cb2));
+      ra = (ca0 * pa0 + ca1 * pa1 + ca2 * pa2) * (cb0 + ca1 + cb2) * inv;
+      rb = (cb0 * pb0 + ca1 * pb1 + cb2 * pb2) * (ca0 + ca1 + ca2) * inv;
+    } else {
+      // float and df64: reciprocal form
+      const T r0 = qrcp<T, FAST>(f0 * f0), r1 = qrcp<T, FAST>(f1 * f1), r2 = qrcp<T, FAST>(f2 * f2);
+      const T ca0 = T(kGqA0) * r0, ca1 = T(kGqA1) * r1, ca2 = T(kGqA2) * r2;
+      const T cb0 = T(kGqA2) * r0, cb2 = T(kGqA0) * r2;
+      ra = qdiv<T, FAST>(ca0 * pa0 + ca1 * pa1 + ca2 * pa2, ca0 + ca1 + ca2);
+      rb = qdiv<T, FAST>(cb0 * pb0 + ca1 * pb1 + cb2 * pb2, cb0 + ca1 + cb2);
+    }
+  } else {
+    T b0, b1, b2;
+    js_betas(q0, q1, q2, q3, q4, b0, b1, b2);
+    const T e0 = weps + b0, e1 = weps + b1, e2 = weps + b2;
+    const T g0 = T(3.0) * q2 - T(4.0) * q3 + q4;
+    const T g2 = T(3.0) * q2 - T(4.0) * q1 + q0;
     const T pa0 = q2 + g0 * S;
     const T pa1 = q2 - (-q1 + q3) * S;
     const T pa2 = q2 - g2 * S;
@@ -369,16 +381,6 @@ __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& r
     const T pb1 = q2 - (q1 - q3) * S;
     const T pb2 = q2 + g2 * S;
     rb = weno_combine<T, FAST>(e0, e1, e2, T(kGqA2), T(kGqA1), T(kGqA0), pb0, pb1, pb2, T(1.0));
-  } else {
-    // float and df64: reciprocal form
-    const T g1 = (q3 - q1) * S;
-    const T pa0 = q2 + g0 * S, pa1 = q2 - g1, pa2 = q2 - g2 * S;
-    const T pb0 = q2 - g0 * S, pb1 = q2 + g1, pb2 = q2 + g2 * S;
-    const T r0 = qrcp<T, FAST>(e0 * e0), r1 = qrcp<T, FAST>(e1 * e1), r2 = qrcp<T, FAST>(e2 * e2);
-    const T ca0 = T(kGqA0) * r0, ca1 = T(kGqA1) * r1, ca2 = T(kGqA2) * r2;
-    const T cb0 = T(kGqA2) * r0, cb2 = T(kGqA0) * r2;
-    ra = qdiv<T, FAST>(ca0 * pa0 + ca1 * pa1 + ca2 * pa2, ca0 + ca1 + ca2);
-    rb = qdiv<T, FAST>(cb0 * pb0 + ca1 * pb1 + cb2 * pb2, cb0 + ca1 + cb2);
   }
 }
 
@@ -558,8 +560,8 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
   if constexpr (!CHAR) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      if constexpr (FAST && is_native_f64<T>) {
-        weno5_lr_fast(c[0][k], c[1][k], c[2][k], c[3][k], c[4][k], c[5][k], weps, ql[k], qr[k]);
+      if constexpr (FAST) {
+        weno5_lr_fast<T>(c[0][k], c[1][k], c[2][k], c[3][k], c[4][k], c[5][k], weps, ql[k], qr[k]);
       } else {
         ql[k] = weno5_left<T, FAST>(c[0][k], c[1][k], c[2][k], c[3][k], c[4][k], weps);
         qr[k] = weno5_right<T, FAST>(c[1][k], c[2][k], c[3][k], c[4][k], c[5][k], weps);
@@ -579,8 +581,8 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
     T chl[4], chr[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      if constexpr (FAST && is_native_f64<T>) {
-        weno5_lr_fast(w[0][k], w[1][k], w[2][k], w[3][k], w[4][k], w[5][k], weps, chl[k], chr[k]);
+      if constexpr (FAST) {
+        weno5_lr_fast<T>(w[0][k], w[1][k], w[2][k], w[3][k], w[4][k], w[5][k], weps, chl[k], chr[k]);
       } else {
         chl[k] = weno5_left<T, FAST>(w[0][k], w[1][k], w[2][k], w[3][k], w[4][k], weps);
         chr[k] = weno5_right<T, FAST>(w[1][k], w[2][k], w[3][k], w[4][k], w[5][k], weps);
