@@ -504,7 +504,7 @@ __device__ __forceinline__ void right_eig(T rho, T u, T v, T h, T c, T R[4][4]) 
 }
 
 // weno.rs:197-205 mat4_vec4: exact mode accumulates every product from 0.0 in
-// column order; FAST skips the structural zeros of the eigenvector matrices.
+// column order (FAST callers use project_left / project_right instead).
 template <class T, bool FAST>
 __device__ __forceinline__ void mat4_vec4(const T M[4][4], const T x[4], T out[4]) {
 #pragma unroll
@@ -518,6 +518,29 @@ __device__ __forceinline__ void mat4_vec4(const T M[4][4], const T x[4], T out[4
       out[r] = M[r][0] * x[0] + M[r][1] * x[1] + M[r][2] * x[2] + M[r][3] * x[3];
     }
   }
+}
+
+// FAST products with the eigenvector matrices that skip their structural
+// zeros (row 2 of L; the zero column entries of R) and unit entries.
+template <class T, bool Y>
+__device__ __forceinline__ void project_left(const T L[4][4], const T x[4], T out[4]) {
+  out[0] = L[0][0] * x[0] + L[0][1] * x[1] + L[0][2] * x[2] + L[0][3] * x[3];
+  out[1] = L[1][0] * x[0] + L[1][1] * x[1] + L[1][2] * x[2] + L[1][3] * x[3];
+  if constexpr (!Y) out[2] = L[2][0] * x[0] + L[2][2] * x[2];
+  else out[2] = L[2][0] * x[0] + L[2][1] * x[1];
+  out[3] = L[3][0] * x[0] + L[3][1] * x[1] + L[3][2] * x[2] + L[3][3] * x[3];
+}
+template <class T, bool Y>
+__device__ __forceinline__ void project_right(const T R[4][4], const T x[4], T out[4]) {
+  out[0] = x[0] + x[1] + x[3];
+  if constexpr (!Y) {
+    out[1] = R[1][0] * x[0] + R[1][1] * x[1] + R[1][3] * x[3];
+    out[2] = R[2][0] * x[0] + R[2][1] * x[1] + R[2][2] * x[2] + R[2][3] * x[3];
+  } else {
+    out[1] = R[1][0] * x[0] + R[1][1] * x[1] + R[1][2] * x[2] + R[1][3] * x[3];
+    out[2] = R[2][0] * x[0] + R[2][1] * x[1] + R[2][3] * x[3];
+  }
+  out[3] = R[3][0] * x[0] + R[3][1] * x[1] + R[3][2] * x[2] + R[3][3] * x[3];
 }
 
 // weno.rs:312-315 pressure ; weno.rs:327-352 Zhang-Shu limiter toward `ub`.
@@ -577,7 +600,10 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
     // cells 2|3), so six projections cover both.
     T w[6][4];
 #pragma unroll
-    for (int s = 0; s < 6; ++s) mat4_vec4<T, FAST>(Lm, c[s], w[s]);
+    for (int s = 0; s < 6; ++s) {
+      if constexpr (FAST) project_left<T, Y>(Lm, c[s], w[s]);
+      else mat4_vec4<T, FAST>(Lm, c[s], w[s]);
+    }
     T chl[4], chr[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -590,8 +616,13 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
     }
     T Rm[4][4];
     right_eig<T, Y>(rho_a, u_a, v_a, h_a, c_a, Rm);
-    mat4_vec4<T, FAST>(Rm, chl, ql);
-    mat4_vec4<T, FAST>(Rm, chr, qr);
+    if constexpr (FAST) {
+      project_right<T, Y>(Rm, chl, ql);
+      project_right<T, Y>(Rm, chr, qr);
+    } else {
+      mat4_vec4<T, FAST>(Rm, chl, ql);
+      mat4_vec4<T, FAST>(Rm, chr, qr);
+    }
     pp_limit<T, FAST>(ql, c[2], gamma);
     pp_limit<T, FAST>(qr, c[3], gamma);
   }
