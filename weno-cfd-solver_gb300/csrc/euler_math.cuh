@@ -37,6 +37,10 @@ constexpr double kSqrt3_12 = 0.1443375673;  // truncated literal, not sqrt(3)/12
 // weno.rs:270 / weno.rs:292 (Gauss-point linear weights, 10 digits)
 constexpr double kGqA0 = 0.1928406937, kGqA1 = 0.6111111111, kGqA2 = 0.1960481952;
 constexpr double kC13 = 13.0 / 12.0;
+// The non-linear weights d_k/(eps+b_k)^2 / sum are unchanged when every
+// eps+b_k is multiplied by the same factor; the FAST forms use 4 (eps+b_k) =
+// 4 eps + (13/3) D^2 + s^2, two fused multiply-adds per indicator.
+constexpr double kC43 = 13.0 / 3.0;
 
 // Arithmetic kinds: native double takes the common-denominator WENO form (its
 // exponent range is ample); float and df64 (float exponent range) take the
@@ -310,13 +314,14 @@ __device__ __forceinline__ void weno5_lr_fast(T u0, T u1, T u2, T u3, T u4, T u5
   // 13/12 D^2 + 1/4 s^2 with s a combination of two first differences.
   const T d0 = u1 - u0, d1 = u2 - u1, d2 = u3 - u2, d3 = u4 - u3, d4 = u5 - u4;
   const T D1 = d1 - d0, D2 = d2 - d1, D3 = d3 - d2, D4 = d4 - d3;
-  const T C1 = T(kC13) * (D1 * D1), C2 = T(kC13) * (D2 * D2), C3 = T(kC13) * (D3 * D3), C4 = T(kC13) * (D4 * D4);
+  // indicators scaled by 4 (see kC43): 4 eps + (13/3) D^2 + s^2
+  const T w4 = T(4.0) * weps;
+  const T C1 = T(kC43) * D1 * D1 + w4, C2 = T(kC43) * D2 * D2 + w4, C3 = T(kC43) * D3 * D3 + w4,
+          C4 = T(kC43) * D4 * D4 + w4;
   const T sl0 = d3 - T(3.0) * d2, sl1 = d1 + d2, sl2 = T(3.0) * d1 - d0;  // left:  stencils 2-4, 1-3, 0-2
   const T sr0 = d4 - T(3.0) * d3, sr1 = d2 + d3, sr2 = T(3.0) * d2 - d1;  // right: stencils 3-5, 2-4, 1-3
-  const T el0 = weps + (C3 + T(0.25) * (sl0 * sl0)), el1 = weps + (C2 + T(0.25) * (sl1 * sl1)),
-          el2 = weps + (C1 + T(0.25) * (sl2 * sl2));
-  const T er0 = weps + (C4 + T(0.25) * (sr0 * sr0)), er1 = weps + (C3 + T(0.25) * (sr1 * sr1)),
-          er2 = weps + (C2 + T(0.25) * (sr2 * sr2));
+  const T el0 = sl0 * sl0 + C3, el1 = sl1 * sl1 + C2, el2 = sl2 * sl2 + C1;
+  const T er0 = sr0 * sr0 + C4, er1 = sr1 * sr1 + C3, er2 = sr2 * sr2 + C2;
   // candidate polynomials (x6): the right stencil's p1, p2 are the left's p0, p1
   const T pl0 = -u4 + T(5.0) * u3 + T(2.0) * u2, pl1 = -u1 + T(5.0) * u2 + T(2.0) * u3;
   const T pl2 = T(2.0) * u0 - T(7.0) * u1 + T(11.0) * u2, pr0 = T(2.0) * u5 - T(7.0) * u4 + T(11.0) * u3;
@@ -344,9 +349,11 @@ __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& r
     const T h0 = d3 - T(3.0) * d2;  // 3 q2 - 4 q3 + q4
     const T h1 = d1 + d2;           // q3 - q1
     const T h2 = T(3.0) * d1 - d0;  // 3 q2 - 4 q1 + q0
-    T f0 = weps + (T(kC13) * (D3 * D3) + T(0.25) * (h0 * h0));
-    T f1 = weps + (T(kC13) * (D2 * D2) + T(0.25) * (h1 * h1));
-    T f2 = weps + (T(kC13) * (D1 * D1) + T(0.25) * (h2 * h2));
+    // indicators scaled by 4 (see kC43): 4 eps + (13/3) D^2 + h^2
+    const T w4 = T(4.0) * weps;
+    T f0 = h0 * h0 + (T(kC43) * D3 * D3 + w4);
+    T f1 = h1 * h1 + (T(kC43) * D2 * D2 + w4);
+    T f2 = h2 * h2 + (T(kC43) * D1 * D1 + w4);
     const T a0 = h0 * S, a1 = h1 * S, a2 = h2 * S;
     const T pa0 = q2 + a0, pa1 = q2 - a1, pa2 = q2 - a2;
     const T pb0 = q2 - a0, pb1 = q2 + a1, pb2 = q2 + a2;
