@@ -258,19 +258,20 @@ __device__ __forceinline__ void weno_nd(double e0, double e1, double e2, double 
   den = (c0 + c1 + c2) * scale;
 }
 
-// x = a/b and y = c/d with one divide, 1/(b d), when b d is a normal number
+// x = a/(k b) and y = c/(k d) with one divide, 1/(k b d), when b d is a normal number
 // well inside the double range (tested on its exponent bits, no FP64 slot);
 // otherwise two divides.
-__device__ __forceinline__ void div_pair(double a, double b, double c, double d, double& x, double& y) {
+__device__ __forceinline__ void div_pair(double a, double b, double c, double d, double& x, double& y,
+                                         double k = 1.0) {
   const double bd = b * d;
   const int e = (__double2hiint(bd) >> 20) & 0x7ff;
   if (e > 64 && e < 1983) {
-    const double inv = 1.0 / bd;
+    const double inv = 1.0 / (bd * k);
     x = a * d * inv;
     y = c * b * inv;
   } else {
-    x = a / b;
-    y = c / d;
+    x = a / (b * k);
+    y = c / (d * k);
   }
 }
 
@@ -326,10 +327,12 @@ __device__ __forceinline__ void weno5_lr_fast(T u0, T u1, T u2, T u3, T u4, T u5
   const T pl0 = -u4 + T(5.0) * u3 + T(2.0) * u2, pl1 = -u1 + T(5.0) * u2 + T(2.0) * u3;
   const T pl2 = T(2.0) * u0 - T(7.0) * u1 + T(11.0) * u2, pr0 = T(2.0) * u5 - T(7.0) * u4 + T(11.0) * u3;
   if constexpr (is_native_f64<T>) {
+    // linear weights scaled by 10 -- (3, 6, 1) and (1, 6, 3) -- and the 1/6 of
+    // the candidate polynomials applied once to the shared divide
     double nl, dl, nr, dr;
-    weno_nd(el0, el1, el2, 0.3, 0.6, 0.1, pl0, pl1, pl2, 6.0, nl, dl);
-    weno_nd(er0, er1, er2, 0.1, 0.6, 0.3, pr0, pl0, pl1, 6.0, nr, dr);
-    div_pair(nl, dl, nr, dr, left, right);
+    weno_nd(el0, el1, el2, 3.0, 6.0, 1.0, pl0, pl1, pl2, 1.0, nl, dl);
+    weno_nd(er0, er1, er2, 1.0, 6.0, 3.0, pr0, pl0, pl1, 1.0, nr, dr);
+    div_pair(nl, dl, nr, dr, left, right, 6.0);
   } else {
     left = weno_combine<T, true>(el0, el1, el2, T(0.3), T(0.6), T(0.1), pl0, pl1, pl2, T(6.0));
     right = weno_combine<T, true>(er0, er1, er2, T(0.1), T(0.6), T(0.3), pr0, pl0, pl1, T(6.0));
@@ -338,6 +341,41 @@ __device__ __forceinline__ void weno5_lr_fast(T u0, T u1, T u2, T u3, T u4, T u5
 
 // weno.rs:262-303: both Gauss-point values from one 5-cell stencil.  The
 // smoothness indicators are shared (the reference recomputes identical values).
+// FAST FP64 Gauss-point pair from the centre value, the slopes h_k of the
+// three candidate polynomials and the (scaled) indicators f_k.
+__device__ __forceinline__ void gq_weights(double q2, double h0, double h1, double h2, double f0, double f1,
+                                           double f2, double& ra, double& rb) {
+  const double S = kSqrt3_12;
+  const double a0 = h0 * S, a1 = h1 * S, a2 = h2 * S;
+  const double pa0 = q2 + a0, pa1 = q2 - a1, pa2 = q2 - a2;
+  const double pb0 = q2 - a0, pb1 = q2 + a1, pb2 = q2 + a2;
+  weno_range(f0, f1, f2);
+  const double s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
+  const double P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
+  // linear weights divided by the centre one (a common factor)
+  const double ca0 = (kGqA0 / kGqA1) * P0, ca1 = P1, ca2 = (kGqA2 / kGqA1) * P2;
+  const double cb0 = (kGqA2 / kGqA1) * P0, cb2 = (kGqA0 / kGqA1) * P2;
+  const double sa = ca0 + ca1 + ca2, sb = cb0 + ca1 + cb2;
+  const double inv = 1.0 / (sa * sb);
+  ra = (ca0 * pa0 + ca1 * pa1 + ca2 * pa2) * sb * inv;
+  rb = (cb0 * pb0 + ca1 * pb1 + cb2 * pb2) * sa * inv;
+}
+
+// Two neighbouring 5-cell stencils (q0..q4 and q1..q5), FAST FP64: both
+// Gauss-point pairs, sharing the first and second differences.
+__device__ __forceinline__ void weno5_gq_two(double q0, double q1, double q2, double q3, double q4, double q5,
+                                             double weps, double& raA, double& rbA, double& raB, double& rbB) {
+  const double d0 = q1 - q0, d1 = q2 - q1, d2 = q3 - q2, d3 = q4 - q3, d4 = q5 - q4;
+  const double D1 = d1 - d0, D2 = d2 - d1, D3 = d3 - d2, D4 = d4 - d3;
+  const double w4 = 4.0 * weps;
+  const double C1 = kC43 * D1 * D1 + w4, C2 = kC43 * D2 * D2 + w4, C3 = kC43 * D3 * D3 + w4,
+               C4 = kC43 * D4 * D4 + w4;
+  const double hA0 = d3 - 3.0 * d2, hA1 = d1 + d2, hA2 = 3.0 * d1 - d0;
+  const double hB0 = d4 - 3.0 * d3, hB1 = d2 + d3, hB2 = 3.0 * d2 - d1;
+  gq_weights(q2, hA0, hA1, hA2, hA0 * hA0 + C3, hA1 * hA1 + C2, hA2 * hA2 + C1, raA, rbA);
+  gq_weights(q3, hB0, hB1, hB2, hB0 * hB0 + C4, hB1 * hB1 + C3, hB2 * hB2 + C2, raB, rbB);
+}
+
 template <class T, bool FAST>
 __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& ra, T& rb, T weps) {
   const T S = T(kSqrt3_12);
@@ -351,23 +389,16 @@ __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& r
     const T h2 = T(3.0) * d1 - d0;  // 3 q2 - 4 q1 + q0
     // indicators scaled by 4 (see kC43): 4 eps + (13/3) D^2 + h^2
     const T w4 = T(4.0) * weps;
-    T f0 = h0 * h0 + (T(kC43) * D3 * D3 + w4);
-    T f1 = h1 * h1 + (T(kC43) * D2 * D2 + w4);
-    T f2 = h2 * h2 + (T(kC43) * D1 * D1 + w4);
-    const T a0 = h0 * S, a1 = h1 * S, a2 = h2 * S;
-    const T pa0 = q2 + a0, pa1 = q2 - a1, pa2 = q2 - a2;
-    const T pb0 = q2 - a0, pb1 = q2 + a1, pb2 = q2 + a2;
+    const T f0 = h0 * h0 + (T(kC43) * D3 * D3 + w4);
+    const T f1 = h1 * h1 + (T(kC43) * D2 * D2 + w4);
+    const T f2 = h2 * h2 + (T(kC43) * D1 * D1 + w4);
     if constexpr (is_native_f64<T>) {
-      weno_range(f0, f1, f2);
-      const T s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
-      const T P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
-      const T ca0 = T(kGqA0) * P0, ca1 = T(kGqA1) * P1, ca2 = T(kGqA2) * P2;
-      const T cb0 = T(kGqA2) * P0, cb2 = T(kGqA0) * P2;
-      const T inv = T(1.0) / ((ca0 + ca1 + ca2) * (cb0 + ca1 + cb2));
-      ra = (ca0 * pa0 + ca1 * pa1 + ca2 * pa2) * (cb0 + ca1 + cb2) * inv;
-      rb = (cb0 * pb0 + ca1 * pb1 + cb2 * pb2) * (ca0 + ca1 + ca2) * inv;
+      gq_weights(q2, h0, h1, h2, f0, f1, f2, ra, rb);
     } else {
       // float and df64: reciprocal form
+      const T a0 = h0 * S, a1 = h1 * S, a2 = h2 * S;
+      const T pa0 = q2 + a0, pa1 = q2 - a1, pa2 = q2 - a2;
+      const T pb0 = q2 - a0, pb1 = q2 + a1, pb2 = q2 + a2;
       const T r0 = qrcp<T, FAST>(f0 * f0), r1 = qrcp<T, FAST>(f1 * f1), r2 = qrcp<T, FAST>(f2 * f2);
       const T ca0 = T(kGqA0) * r0, ca1 = T(kGqA1) * r1, ca2 = T(kGqA2) * r2;
       const T cb0 = T(kGqA2) * r0, cb2 = T(kGqA0) * r2;

@@ -117,30 +117,10 @@ __device__ __forceinline__ void gq_face(const Planes<T>& P, int64_t row, int64_t
   }
 }
 
+// The Riemann solver and the stores of one pass-2 face (row, col).
 template <class T, bool FAST, bool Y, int OUT>
-__global__ void __launch_bounds__(128) k_pass2(Planes<T> PL, Planes<T> PR, int64_t rows, int64_t cols, T gamma,
-                                                Pass2Dst dst, T weps) {
-  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t row = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
-  if (row >= rows || col >= cols) return;
-  T ql[4], qr[4], fl[4], fr[4];
-  {
-    T a1[4], a2[4], f1[4], f2[4];
-    gq_face<T, FAST, Y>(PL, row, col, a1, a2, weps);
-    euler_flux_pair<T, FAST, Y>(a1, a2, gamma, f1, f2);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      fl[k] = T(0.5) * (f1[k] + f2[k]);
-      ql[k] = T(0.5) * (a1[k] + a2[k]);
-    }
-    gq_face<T, FAST, Y>(PR, row, col, a1, a2, weps);
-    euler_flux_pair<T, FAST, Y>(a1, a2, gamma, f1, f2);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      fr[k] = T(0.5) * (f2[k] + f1[k]);
-      qr[k] = T(0.5) * (a1[k] + a2[k]);
-    }
-  }
+__device__ __forceinline__ void pass2_emit(const T ql[4], const T fl[4], const T qr[4], const T fr[4], T gamma,
+                                           const Pass2Dst& dst, int64_t row, int64_t col, int64_t cols) {
   const int64_t e = row * dst.ld + col;
   if constexpr (OUT == P2_STATES) {
     const int64_t o = (row * cols + col) * 4;
@@ -171,6 +151,81 @@ __global__ void __launch_bounds__(128) k_pass2(Planes<T> PL, Planes<T> PR, int64
       static_cast<T*>(dst.c)[e] = T(0.5) * (r.p_l + r.p_r);
     }
   }
+}
+
+template <class T, bool FAST, bool Y, int OUT>
+__global__ void __launch_bounds__(128) k_pass2(Planes<T> PL, Planes<T> PR, int64_t rows, int64_t cols, T gamma,
+                                                Pass2Dst dst, T weps) {
+  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t row = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
+  if (row >= rows || col >= cols) return;
+  T ql[4], qr[4], fl[4], fr[4];
+  {
+    T a1[4], a2[4], f1[4], f2[4];
+    gq_face<T, FAST, Y>(PL, row, col, a1, a2, weps);
+    euler_flux_pair<T, FAST, Y>(a1, a2, gamma, f1, f2);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      fl[k] = T(0.5) * (f1[k] + f2[k]);
+      ql[k] = T(0.5) * (a1[k] + a2[k]);
+    }
+    gq_face<T, FAST, Y>(PR, row, col, a1, a2, weps);
+    euler_flux_pair<T, FAST, Y>(a1, a2, gamma, f1, f2);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      fr[k] = T(0.5) * (f2[k] + f1[k]);
+      qr[k] = T(0.5) * (a1[k] + a2[k]);
+    }
+  }
+  pass2_emit<T, FAST, Y, OUT>(ql, fl, qr, fr, gamma, dst, row, col, cols);
+}
+
+// Face-averaged states and fluxes of two neighbouring faces (along the
+// transverse direction) from one side's pass-1 planes, FAST FP64.
+template <bool Y>
+__device__ __forceinline__ void gq_side_two(const Planes<double>& P, int64_t row, int64_t col, double gamma,
+                                            double weps, double qA[4], double fA[4], double qB[4], double fB[4]) {
+  double a1A[4], a2A[4], a1B[4], a2B[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    double v[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) v[t] = Y ? P.at(k, row + 1 + t, col) : P.at(k, row, col + 1 + t);
+    weno5_gq_two(v[0], v[1], v[2], v[3], v[4], v[5], weps, a1A[k], a2A[k], a1B[k], a2B[k]);
+  }
+  double f1[4], f2[4];
+  euler_flux_pair<double, true, Y>(a1A, a2A, gamma, f1, f2);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    fA[k] = 0.5 * (f1[k] + f2[k]);
+    qA[k] = 0.5 * (a1A[k] + a2A[k]);
+  }
+  euler_flux_pair<double, true, Y>(a1B, a2B, gamma, f1, f2);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    fB[k] = 0.5 * (f1[k] + f2[k]);
+    qB[k] = 0.5 * (a1B[k] + a2B[k]);
+  }
+}
+
+// FAST FP64 pass 2 with two faces per thread along the transverse direction
+// (columns for the x sweep, rows for the y sweep): the six transverse values
+// of each component serve both faces, whose Gauss-point reconstructions share
+// their first and second differences.
+template <bool Y, int OUT>
+__global__ void __launch_bounds__(128) k_pass2_two(Planes<double> PL, Planes<double> PR, int64_t rows, int64_t cols,
+                                                    double gamma, Pass2Dst dst, double weps) {
+  int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t row = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
+  if constexpr (Y) row *= 2;
+  else col *= 2;
+  if (row >= rows || col >= cols) return;
+  const bool two = Y ? (row + 1 < rows) : (col + 1 < cols);
+  double qlA[4], flA[4], qlB[4], flB[4], qrA[4], frA[4], qrB[4], frB[4];
+  gq_side_two<Y>(PL, row, col, gamma, weps, qlA, flA, qlB, flB);
+  gq_side_two<Y>(PR, row, col, gamma, weps, qrA, frA, qrB, frB);
+  pass2_emit<double, true, Y, OUT>(qlA, flA, qrA, frA, gamma, dst, row, col, cols);
+  if (two) pass2_emit<double, true, Y, OUT>(qlB, flB, qrB, frB, gamma, dst, Y ? row + 1 : row, Y ? col : col + 1, cols);
 }
 
 // Riemann solver on caller-provided dense (rows, cols, 4) face arrays

@@ -57,6 +57,22 @@ cudaError_t Launch<T, FAST>::pass2(HostPlanes PL, HostPlanes PR, int64_t rows, i
   auto L = planes<T>(PL), R = planes<T>(PR);
   Pass2Dst dst{a, b, c, d, ps, ld};
   const T gm = (T)gamma;
+  if constexpr (FAST && std::is_same<T, double>::value) {
+    // two faces per thread along the transverse direction
+    const dim3 g2 = ydir ? grid2d((rows + 1) / 2, cols, kBlk) : grid2d(rows, (cols + 1) / 2, kBlk);
+#define WENO_P2T(Y, K) k_pass2_two<Y, K><<<g2, kBlk, 0, st>>>(L, R, rows, cols, gm, dst, (T)weps)
+    if (!ydir) {
+      if (kind == 0) WENO_P2T(false, P2_STATES);
+      else if (kind == 1) WENO_P2T(false, P2_HLLE);
+      else WENO_P2T(false, P2_BLEND);
+    } else {
+      if (kind == 0) WENO_P2T(true, P2_STATES);
+      else if (kind == 1) WENO_P2T(true, P2_HLLE);
+      else WENO_P2T(true, P2_BLEND);
+    }
+#undef WENO_P2T
+    return cudaGetLastError();
+  }
 #define WENO_P2(Y, K) k_pass2<T, FAST, Y, K><<<g, kBlk, 0, st>>>(L, R, rows, cols, gm, dst, (T)weps)
   if (!ydir) {
     if (kind == 0) WENO_P2(false, P2_STATES);
