@@ -558,27 +558,41 @@ __device__ __forceinline__ void mat4_vec4(const T M[4][4], const T x[4], T out[4
   }
 }
 
-// FAST products with the eigenvector matrices that skip their structural
-// zeros (row 2 of L; the zero column entries of R) and unit entries.
+// FAST products with the eigenvector matrices of weno.rs:76-189, written from
+// their structure instead of a 4x4 product.  With G = (gamma-1)/c^2,
+// kin = (u^2+v^2)/2, b = u_n/(2c), hr = 1/(2 rho c) and Z = kin q0 - u q1 - v q2 + q3:
+//   L q = ( G Z/2 + (b q0 - hr q_n),  q0 - G Z,  (q_t - u_t q0)/rho,  G Z/2 - (b q0 - hr q_n) )
+// (n the normal and t the tangential momentum index), and with s = w0+w1+w3:
+//   R w = ( s,  u s + [c (w3-w0) | rho w2],  v s + [rho w2 | c (w3-w0)],  R3 . w ).
+template <class T>
+struct CharScalars {
+  T u, v, c, rho, irho, kin, G, G2, b, hr, h;
+};
+
 template <class T, bool Y>
-__device__ __forceinline__ void project_left(const T L[4][4], const T x[4], T out[4]) {
-  out[0] = L[0][0] * x[0] + L[0][1] * x[1] + L[0][2] * x[2] + L[0][3] * x[3];
-  out[1] = L[1][0] * x[0] + L[1][1] * x[1] + L[1][2] * x[2] + L[1][3] * x[3];
-  if constexpr (!Y) out[2] = L[2][0] * x[0] + L[2][2] * x[2];
-  else out[2] = L[2][0] * x[0] + L[2][1] * x[1];
-  out[3] = L[3][0] * x[0] + L[3][1] * x[1] + L[3][2] * x[2] + L[3][3] * x[3];
+__device__ __forceinline__ void project_left(const CharScalars<T>& k, const T q[4], T w[4]) {
+  const T Z = k.kin * q[0] - k.u * q[1] - k.v * q[2] + q[3];
+  const T X = k.G2 * Z;
+  const T Yv = k.b * q[0] - k.hr * q[Y ? 2 : 1];
+  w[0] = X + Yv;
+  w[1] = q[0] - k.G * Z;
+  w[2] = k.irho * (q[Y ? 1 : 2] - (Y ? k.u : k.v) * q[0]);
+  w[3] = X - Yv;
 }
 template <class T, bool Y>
-__device__ __forceinline__ void project_right(const T R[4][4], const T x[4], T out[4]) {
-  out[0] = x[0] + x[1] + x[3];
+__device__ __forceinline__ void project_right(const CharScalars<T>& k, const T w[4], T out[4]) {
+  const T s = w[0] + w[1] + w[3];
+  const T d = w[3] - w[0];
+  const T un = Y ? k.v : k.u;
+  out[0] = s;
   if constexpr (!Y) {
-    out[1] = R[1][0] * x[0] + R[1][1] * x[1] + R[1][3] * x[3];
-    out[2] = R[2][0] * x[0] + R[2][1] * x[1] + R[2][2] * x[2] + R[2][3] * x[3];
+    out[1] = k.u * s + k.c * d;
+    out[2] = k.v * s + k.rho * w[2];
   } else {
-    out[1] = R[1][0] * x[0] + R[1][1] * x[1] + R[1][2] * x[2] + R[1][3] * x[3];
-    out[2] = R[2][0] * x[0] + R[2][1] * x[1] + R[2][3] * x[3];
+    out[1] = k.u * s + k.rho * w[2];
+    out[2] = k.v * s + k.c * d;
   }
-  out[3] = R[3][0] * x[0] + R[3][1] * x[1] + R[3][2] * x[2] + R[3][3] * x[3];
+  out[3] = (k.h - un * k.c) * w[0] + k.kin * w[1] + (k.rho * (Y ? k.u : k.v)) * w[2] + (k.h + un * k.c) * w[3];
 }
 
 // weno.rs:312-315 pressure ; weno.rs:327-352 Zhang-Shu limiter toward `ub`.
@@ -631,33 +645,42 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
   } else {
     T rho_a, u_a, v_a, h_a, c_a, ic_a = T(0.0), irho_a = T(0.0);
     roe_avg<T, FAST>(c[2], c[3], gamma, rho_a, u_a, v_a, h_a, c_a, ic_a, irho_a);
-    T Lm[4][4];
-    left_eig<T, FAST, Y>(rho_a, u_a, v_a, c_a, gamma, Lm, ic_a, irho_a);
     // The reference projects cells 0..4 for the left state and 1..5 for the
     // right state with the same matrix (both faces use the Roe average of
     // cells 2|3), so six projections cover both.
     T w[6][4];
-#pragma unroll
-    for (int s = 0; s < 6; ++s) {
-      if constexpr (FAST) project_left<T, Y>(Lm, c[s], w[s]);
-      else mat4_vec4<T, FAST>(Lm, c[s], w[s]);
-    }
     T chl[4], chr[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      if constexpr (FAST) {
-        weno5_lr_fast<T>(w[0][k], w[1][k], w[2][k], w[3][k], w[4][k], w[5][k], weps, chl[k], chr[k]);
-      } else {
-        chl[k] = weno5_left<T, FAST>(w[0][k], w[1][k], w[2][k], w[3][k], w[4][k], weps);
-        chr[k] = weno5_right<T, FAST>(w[1][k], w[2][k], w[3][k], w[4][k], w[5][k], weps);
-      }
-    }
-    T Rm[4][4];
-    right_eig<T, Y>(rho_a, u_a, v_a, h_a, c_a, Rm);
     if constexpr (FAST) {
-      project_right<T, Y>(Rm, chl, ql);
-      project_right<T, Y>(Rm, chr, qr);
+      CharScalars<T> k;
+      k.u = u_a;
+      k.v = v_a;
+      k.c = c_a;
+      k.rho = rho_a;
+      k.irho = irho_a;
+      k.h = h_a;
+      k.kin = T(0.5) * (u_a * u_a + v_a * v_a);
+      k.G = (gamma - T(1.0)) * (ic_a * ic_a);
+      k.G2 = T(0.5) * k.G;
+      k.b = T(0.5) * (Y ? v_a : u_a) * ic_a;
+      k.hr = T(0.5) * (ic_a * irho_a);
+#pragma unroll
+      for (int s = 0; s < 6; ++s) project_left<T, Y>(k, c[s], w[s]);
+#pragma unroll
+      for (int f = 0; f < 4; ++f) weno5_lr_fast<T>(w[0][f], w[1][f], w[2][f], w[3][f], w[4][f], w[5][f], weps, chl[f], chr[f]);
+      project_right<T, Y>(k, chl, ql);
+      project_right<T, Y>(k, chr, qr);
     } else {
+      T Lm[4][4];
+      left_eig<T, FAST, Y>(rho_a, u_a, v_a, c_a, gamma, Lm, ic_a, irho_a);
+#pragma unroll
+      for (int s = 0; s < 6; ++s) mat4_vec4<T, FAST>(Lm, c[s], w[s]);
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        chl[f] = weno5_left<T, FAST>(w[0][f], w[1][f], w[2][f], w[3][f], w[4][f], weps);
+        chr[f] = weno5_right<T, FAST>(w[1][f], w[2][f], w[3][f], w[4][f], w[5][f], weps);
+      }
+      T Rm[4][4];
+      right_eig<T, Y>(rho_a, u_a, v_a, h_a, c_a, Rm);
       mat4_vec4<T, FAST>(Rm, chl, ql);
       mat4_vec4<T, FAST>(Rm, chr, qr);
     }
