@@ -341,39 +341,49 @@ __device__ __forceinline__ void weno5_lr_fast(T u0, T u1, T u2, T u3, T u4, T u5
 
 // weno.rs:262-303: both Gauss-point values from one 5-cell stencil.  The
 // smoothness indicators are shared (the reference recomputes identical values).
-// FAST FP64 Gauss-point pair from the centre value, the slopes h_k of the
-// three candidate polynomials and the (scaled) indicators f_k.
-__device__ __forceinline__ void gq_weights(double q2, double h0, double h1, double h2, double f0, double f1,
-                                           double f2, double& ra, double& rb) {
-  const double S = kSqrt3_12;
-  const double a0 = h0 * S, a1 = h1 * S, a2 = h2 * S;
-  const double pa0 = q2 + a0, pa1 = q2 - a1, pa2 = q2 - a2;
-  const double pb0 = q2 - a0, pb1 = q2 + a1, pb2 = q2 + a2;
-  weno_range(f0, f1, f2);
-  const double s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
-  const double P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
-  // linear weights divided by the centre one (a common factor)
-  const double ca0 = (kGqA0 / kGqA1) * P0, ca1 = P1, ca2 = (kGqA2 / kGqA1) * P2;
-  const double cb0 = (kGqA2 / kGqA1) * P0, cb2 = (kGqA0 / kGqA1) * P2;
-  const double sa = ca0 + ca1 + ca2, sb = cb0 + ca1 + cb2;
-  const double inv = 1.0 / (sa * sb);
-  ra = (ca0 * pa0 + ca1 * pa1 + ca2 * pa2) * sb * inv;
-  rb = (cb0 * pb0 + ca1 * pb1 + cb2 * pb2) * sa * inv;
+// FAST Gauss-point pair from the centre value, the slopes h_k of the three
+// candidate polynomials and the (scaled) indicators f_k: native double in the
+// common-denominator form, float and df64 with reciprocals.
+template <class T>
+__device__ __forceinline__ void gq_weights(T q2, T h0, T h1, T h2, T f0, T f1, T f2, T& ra, T& rb) {
+  const T S = T(kSqrt3_12);
+  const T a0 = h0 * S, a1 = h1 * S, a2 = h2 * S;
+  const T pa0 = q2 + a0, pa1 = q2 - a1, pa2 = q2 - a2;
+  const T pb0 = q2 - a0, pb1 = q2 + a1, pb2 = q2 + a2;
+  if constexpr (is_native_f64<T>) {
+    weno_range(f0, f1, f2);
+    const double s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
+    const double P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
+    // linear weights divided by the centre one (a common factor)
+    const double ca0 = (kGqA0 / kGqA1) * P0, ca1 = P1, ca2 = (kGqA2 / kGqA1) * P2;
+    const double cb0 = (kGqA2 / kGqA1) * P0, cb2 = (kGqA0 / kGqA1) * P2;
+    const double sa = ca0 + ca1 + ca2, sb = cb0 + ca1 + cb2;
+    const double inv = 1.0 / (sa * sb);
+    ra = (ca0 * pa0 + ca1 * pa1 + ca2 * pa2) * sb * inv;
+    rb = (cb0 * pb0 + ca1 * pb1 + cb2 * pb2) * sa * inv;
+  } else {
+    const T r0 = qrcp<T, true>(f0 * f0), r1 = qrcp<T, true>(f1 * f1), r2 = qrcp<T, true>(f2 * f2);
+    const T ca0 = T(kGqA0 / kGqA1) * r0, ca1 = r1, ca2 = T(kGqA2 / kGqA1) * r2;
+    const T cb0 = T(kGqA2 / kGqA1) * r0, cb2 = T(kGqA0 / kGqA1) * r2;
+    ra = qdiv<T, true>(ca0 * pa0 + ca1 * pa1 + ca2 * pa2, ca0 + ca1 + ca2);
+    rb = qdiv<T, true>(cb0 * pb0 + ca1 * pb1 + cb2 * pb2, cb0 + ca1 + cb2);
+  }
 }
 
-// Two neighbouring 5-cell stencils (q0..q4 and q1..q5), FAST FP64: both
+// Two neighbouring 5-cell stencils (q0..q4 and q1..q5), FAST: both
 // Gauss-point pairs, sharing the first and second differences.
-__device__ __forceinline__ void weno5_gq_two(double q0, double q1, double q2, double q3, double q4, double q5,
-                                             double weps, double& raA, double& rbA, double& raB, double& rbB) {
-  const double d0 = q1 - q0, d1 = q2 - q1, d2 = q3 - q2, d3 = q4 - q3, d4 = q5 - q4;
-  const double D1 = d1 - d0, D2 = d2 - d1, D3 = d3 - d2, D4 = d4 - d3;
-  const double w4 = 4.0 * weps;
-  const double C1 = kC43 * D1 * D1 + w4, C2 = kC43 * D2 * D2 + w4, C3 = kC43 * D3 * D3 + w4,
-               C4 = kC43 * D4 * D4 + w4;
-  const double hA0 = d3 - 3.0 * d2, hA1 = d1 + d2, hA2 = 3.0 * d1 - d0;
-  const double hB0 = d4 - 3.0 * d3, hB1 = d2 + d3, hB2 = 3.0 * d2 - d1;
-  gq_weights(q2, hA0, hA1, hA2, hA0 * hA0 + C3, hA1 * hA1 + C2, hA2 * hA2 + C1, raA, rbA);
-  gq_weights(q3, hB0, hB1, hB2, hB0 * hB0 + C4, hB1 * hB1 + C3, hB2 * hB2 + C2, raB, rbB);
+template <class T>
+__device__ __forceinline__ void weno5_gq_two(T q0, T q1, T q2, T q3, T q4, T q5, T weps, T& raA, T& rbA, T& raB,
+                                             T& rbB) {
+  const T d0 = q1 - q0, d1 = q2 - q1, d2 = q3 - q2, d3 = q4 - q3, d4 = q5 - q4;
+  const T D1 = d1 - d0, D2 = d2 - d1, D3 = d3 - d2, D4 = d4 - d3;
+  const T w4 = T(4.0) * weps;
+  const T C1 = T(kC43) * D1 * D1 + w4, C2 = T(kC43) * D2 * D2 + w4, C3 = T(kC43) * D3 * D3 + w4,
+          C4 = T(kC43) * D4 * D4 + w4;
+  const T hA0 = d3 - T(3.0) * d2, hA1 = d1 + d2, hA2 = T(3.0) * d1 - d0;
+  const T hB0 = d4 - T(3.0) * d3, hB1 = d2 + d3, hB2 = T(3.0) * d2 - d1;
+  gq_weights<T>(q2, hA0, hA1, hA2, hA0 * hA0 + C3, hA1 * hA1 + C2, hA2 * hA2 + C1, raA, rbA);
+  gq_weights<T>(q3, hB0, hB1, hB2, hB0 * hB0 + C4, hB1 * hB1 + C3, hB2 * hB2 + C2, raB, rbB);
 }
 
 template <class T, bool FAST>
@@ -392,19 +402,7 @@ __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& r
     const T f0 = h0 * h0 + (T(kC43) * D3 * D3 + w4);
     const T f1 = h1 * h1 + (T(kC43) * D2 * D2 + w4);
     const T f2 = h2 * h2 + (T(kC43) * D1 * D1 + w4);
-    if constexpr (is_native_f64<T>) {
-      gq_weights(q2, h0, h1, h2, f0, f1, f2, ra, rb);
-    } else {
-      // float and df64: reciprocal form
-      const T a0 = h0 * S, a1 = h1 * S, a2 = h2 * S;
-      const T pa0 = q2 + a0, pa1 = q2 - a1, pa2 = q2 - a2;
-      const T pb0 = q2 - a0, pb1 = q2 + a1, pb2 = q2 + a2;
-      const T r0 = qrcp<T, FAST>(f0 * f0), r1 = qrcp<T, FAST>(f1 * f1), r2 = qrcp<T, FAST>(f2 * f2);
-      const T ca0 = T(kGqA0) * r0, ca1 = T(kGqA1) * r1, ca2 = T(kGqA2) * r2;
-      const T cb0 = T(kGqA2) * r0, cb2 = T(kGqA0) * r2;
-      ra = qdiv<T, FAST>(ca0 * pa0 + ca1 * pa1 + ca2 * pa2, ca0 + ca1 + ca2);
-      rb = qdiv<T, FAST>(cb0 * pb0 + ca1 * pb1 + cb2 * pb2, cb0 + ca1 + cb2);
-    }
+    gq_weights<T>(q2, h0, h1, h2, f0, f1, f2, ra, rb);
   } else {
     T b0, b1, b2;
     js_betas(q0, q1, q2, q3, q4, b0, b1, b2);

@@ -181,51 +181,51 @@ __global__ void __launch_bounds__(128) k_pass2(Planes<T> PL, Planes<T> PR, int64
 }
 
 // Face-averaged states and fluxes of two neighbouring faces (along the
-// transverse direction) from one side's pass-1 planes, FAST FP64.
-template <bool Y>
-__device__ __forceinline__ void gq_side_two(const Planes<double>& P, int64_t row, int64_t col, double gamma,
-                                            double weps, double qA[4], double fA[4], double qB[4], double fB[4]) {
-  double a1A[4], a2A[4], a1B[4], a2B[4];
+// transverse direction) from one side's pass-1 planes, FAST arithmetic.
+template <class T, bool Y>
+__device__ __forceinline__ void gq_side_two(const Planes<T>& P, int64_t row, int64_t col, T gamma, T weps, T qA[4],
+                                            T fA[4], T qB[4], T fB[4]) {
+  T a1A[4], a2A[4], a1B[4], a2B[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    double v[6];
+    T v[6];
 #pragma unroll
     for (int t = 0; t < 6; ++t) v[t] = Y ? P.at(k, row + 1 + t, col) : P.at(k, row, col + 1 + t);
-    weno5_gq_two(v[0], v[1], v[2], v[3], v[4], v[5], weps, a1A[k], a2A[k], a1B[k], a2B[k]);
+    weno5_gq_two<T>(v[0], v[1], v[2], v[3], v[4], v[5], weps, a1A[k], a2A[k], a1B[k], a2B[k]);
   }
-  double f1[4], f2[4];
-  euler_flux_pair<double, true, Y>(a1A, a2A, gamma, f1, f2);
+  T f1[4], f2[4];
+  euler_flux_pair<T, true, Y>(a1A, a2A, gamma, f1, f2);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    fA[k] = 0.5 * (f1[k] + f2[k]);
-    qA[k] = 0.5 * (a1A[k] + a2A[k]);
+    fA[k] = T(0.5) * (f1[k] + f2[k]);
+    qA[k] = T(0.5) * (a1A[k] + a2A[k]);
   }
-  euler_flux_pair<double, true, Y>(a1B, a2B, gamma, f1, f2);
+  euler_flux_pair<T, true, Y>(a1B, a2B, gamma, f1, f2);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    fB[k] = 0.5 * (f1[k] + f2[k]);
-    qB[k] = 0.5 * (a1B[k] + a2B[k]);
+    fB[k] = T(0.5) * (f1[k] + f2[k]);
+    qB[k] = T(0.5) * (a1B[k] + a2B[k]);
   }
 }
 
-// FAST FP64 pass 2 with two faces per thread along the transverse direction
+// FAST pass 2 with two faces per thread along the transverse direction
 // (columns for the x sweep, rows for the y sweep): the six transverse values
 // of each component serve both faces, whose Gauss-point reconstructions share
 // their first and second differences.
-template <bool Y, int OUT>
-__global__ void __launch_bounds__(128) k_pass2_two(Planes<double> PL, Planes<double> PR, int64_t rows, int64_t cols,
-                                                    double gamma, Pass2Dst dst, double weps) {
+template <class T, bool Y, int OUT>
+__global__ void __launch_bounds__(128) k_pass2_two(Planes<T> PL, Planes<T> PR, int64_t rows, int64_t cols, T gamma,
+                                                    Pass2Dst dst, T weps) {
   int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t row = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
   if constexpr (Y) row *= 2;
   else col *= 2;
   if (row >= rows || col >= cols) return;
   const bool two = Y ? (row + 1 < rows) : (col + 1 < cols);
-  double qlA[4], flA[4], qlB[4], flB[4], qrA[4], frA[4], qrB[4], frB[4];
-  gq_side_two<Y>(PL, row, col, gamma, weps, qlA, flA, qlB, flB);
-  gq_side_two<Y>(PR, row, col, gamma, weps, qrA, frA, qrB, frB);
-  pass2_emit<double, true, Y, OUT>(qlA, flA, qrA, frA, gamma, dst, row, col, cols);
-  if (two) pass2_emit<double, true, Y, OUT>(qlB, flB, qrB, frB, gamma, dst, Y ? row + 1 : row, Y ? col : col + 1, cols);
+  T qlA[4], flA[4], qlB[4], flB[4], qrA[4], frA[4], qrB[4], frB[4];
+  gq_side_two<T, Y>(PL, row, col, gamma, weps, qlA, flA, qlB, flB);
+  gq_side_two<T, Y>(PR, row, col, gamma, weps, qrA, frA, qrB, frB);
+  pass2_emit<T, true, Y, OUT>(qlA, flA, qrA, frA, gamma, dst, row, col, cols);
+  if (two) pass2_emit<T, true, Y, OUT>(qlB, flB, qrB, frB, gamma, dst, Y ? row + 1 : row, Y ? col : col + 1, cols);
 }
 
 // Riemann solver on caller-provided dense (rows, cols, 4) face arrays

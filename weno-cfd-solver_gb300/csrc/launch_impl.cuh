@@ -57,10 +57,11 @@ cudaError_t Launch<T, FAST>::pass2(HostPlanes PL, HostPlanes PR, int64_t rows, i
   auto L = planes<T>(PL), R = planes<T>(PR);
   Pass2Dst dst{a, b, c, d, ps, ld};
   const T gm = (T)gamma;
-  if constexpr (FAST && std::is_same<T, double>::value) {
-    // two faces per thread along the transverse direction
+  if constexpr (FAST && !std::is_same<T, df64>::value) {
+    // two faces per thread along the transverse direction (df64 keeps one:
+    // its larger per-face register footprint outweighs the shared differences)
     const dim3 g2 = ydir ? grid2d((rows + 1) / 2, cols, kBlk) : grid2d(rows, (cols + 1) / 2, kBlk);
-#define WENO_P2T(Y, K) k_pass2_two<Y, K><<<g2, kBlk, 0, st>>>(L, R, rows, cols, gm, dst, (T)weps)
+#define WENO_P2T(Y, K) k_pass2_two<T, Y, K><<<g2, kBlk, 0, st>>>(L, R, rows, cols, gm, dst, (T)weps)
     if (!ydir) {
       if (kind == 0) WENO_P2T(false, P2_STATES);
       else if (kind == 1) WENO_P2T(false, P2_HLLE);
