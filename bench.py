@@ -551,6 +551,11 @@ def main():
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"}
+    pipe = prof.get("fp64_pipe_pct_of_peak") if args.precision == "f64" else None
+    if pipe:
+        # The HBM fraction is the contract's denominator; the pipe that binds these kernels is FP64.
+        roofline["binding"] = {"pipe": "fp64", "ncu_fp64_pipe_pct": pipe,
+                               "source": "profiles/k_pass1_k_pass2_fp64_fast_2048.md (ncu, 2048^2)"}
     r64, rdiv, r32 = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
     _lib.check(L.weno_probe_rates(ctypes.byref(r64), ctypes.byref(rdiv), ctypes.byref(r32), None), "probe")
     flops = load_json(os.path.join(ROOT, "profiles", "flops_per_cell.json")) or {}
