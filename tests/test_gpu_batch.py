@@ -121,3 +121,24 @@ def test_pool_full_and_slots(wx, orc):
     b.add(small, 0.1)
     with pytest.raises(ValueError):
         b.add(small, 0.1)  # both slots used
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_pool_cells_is_exact(wx, orc, precision):
+    """Batch.pool_cells sizes a pool that holds exactly the given solves (rows padded
+    to 16 bytes for the tile loads); one cell less does not."""
+    rng = np.random.default_rng(13)
+    shapes = [(37, 53), (64, 30), (19, 101)]  # row lengths not multiples of 16 bytes
+    states = [synced(orc, quadrant(rng, nx, ny)) for nx, ny in shapes]
+    cells = wx.Batch.pool_cells(shapes, precision)
+    b = wx.Batch(cells, len(shapes), precision=precision, mode="fast")
+    for (nx, ny), q in zip(shapes, states):
+        b.add(q, 1.0 / max(nx, ny), max_steps=2)
+    assert b.stats()["free_cells"] == 0
+    b.run(2)
+    for s in range(len(shapes)):
+        assert b.info(s)["steps"] == 2 and b.info(s)["status"] == 0
+    short = wx.Batch(cells - 16, len(shapes), precision=precision, mode="fast")
+    with pytest.raises(ValueError):
+        for (nx, ny), q in zip(shapes, states):
+            short.add(q, 1.0 / max(nx, ny))

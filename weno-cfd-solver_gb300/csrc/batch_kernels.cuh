@@ -146,6 +146,29 @@ __device__ __forceinline__ T tile_sensor(const T* pbar, int R, int C, int fr, in
   return sensor_weight<T, FAST>(dpdx, dpdy, p, jp_lo, jp_hi);
 }
 
+// Riemann solver of one tile face and its store into the face buffer F
+// (HLLE flux planes, or HLLC + HLLE + mean pressure for the sensor blend).
+template <class T, bool FAST, bool Y, bool BLEND>
+__device__ __forceinline__ void tile_face_flux(const T ql[4], const T fl[4], const T qr[4], const T fr[4], T gamma,
+                                               T* F, int FN, int e) {
+  const RiemannPre<T, FAST, Y> rp = riemann_pre<T, FAST, Y>(ql, qr, gamma);
+  T H[4];
+  hlle_flux<T, FAST, Y>(rp, ql, fl, qr, fr, H);
+  if constexpr (BLEND) {
+    T Gc[4];
+    hllc_flux<T, FAST, Y>(rp, ql, fl, qr, fr, Gc);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      F[k * FN + e] = Gc[k];
+      F[(4 + k) * FN + e] = H[k];
+    }
+    F[8 * FN + e] = T(0.5) * (rp.p_l + rp.p_r);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) F[k * FN + e] = H[k];
+  }
+}
+
 // One SSP-RK3 stage (1..3) for every tile of the list.  The stage input (pool
 // stage-1 of q, q1, q2) is read through each solve's tensor map `tmaps[solve]`;
 // Qn is the step's initial state, Qo the output pool.
@@ -281,23 +304,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
           qr[k] = T(0.5) * (a1[k] + a2[k]);
         }
       }
-      const RiemannPre<T, FAST, false> rp = riemann_pre<T, FAST, false>(ql, qr, gamma);
-      T F[4];
-      hlle_flux<T, FAST, false>(rp, ql, fl, qr, fr_, F);
-      const int FN = G::FXR * G::FXC;
-      if constexpr (BLEND) {
-        T Gc[4];
-        hllc_flux<T, FAST, false>(rp, ql, fl, qr, fr_, Gc);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          FX[k * FN + e] = Gc[k];
-          FX[(4 + k) * FN + e] = F[k];
-        }
-        FX[8 * FN + e] = T(0.5) * (rp.p_l + rp.p_r);
-      } else {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) FX[k * FN + e] = F[k];
-      }
+      tile_face_flux<T, FAST, false, BLEND>(ql, fl, qr, fr_, gamma, FX, G::FXR * G::FXC, e);
     }
     __syncthreads();
     // ---- x flux difference of every cell of the tile (sensor blend of the x faces) ----
@@ -380,23 +387,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
           qr[k] = T(0.5) * (a1[k] + a2[k]);
         }
       }
-      const RiemannPre<T, FAST, true> rp = riemann_pre<T, FAST, true>(ql, qr, gamma);
-      T F[4];
-      hlle_flux<T, FAST, true>(rp, ql, fl, qr, fr_, F);
-      const int FN = G::FYR * G::FYC;
-      if constexpr (BLEND) {
-        T Gc[4];
-        hllc_flux<T, FAST, true>(rp, ql, fl, qr, fr_, Gc);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          FY[k * FN + e] = Gc[k];
-          FY[(4 + k) * FN + e] = F[k];
-        }
-        FY[8 * FN + e] = T(0.5) * (rp.p_l + rp.p_r);
-      } else {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) FY[k * FN + e] = F[k];
-      }
+      tile_face_flux<T, FAST, true, BLEND>(ql, fl, qr, fr_, gamma, FY, G::FYR * G::FYC, e);
     }
     __syncthreads();
 
