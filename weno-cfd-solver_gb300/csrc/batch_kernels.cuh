@@ -441,13 +441,22 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
         qo[k * ps + o] = v[k];
       }
       if (stage == 3) {
-        // Rie_prob_2d_rs.py:312-315 on the new state (primitives as con2primi writes them)
-        const double r0 = (double)v[0];
-        const double rho = fmax(r0, kEps);
-        const double uu = (double)v[1] / rho, vv = (double)v[2] / rho;
-        const double pp = fmax(((double)gamma - 1.0) * ((double)v[3] - 0.5 * rho * (uu * uu + vv * vv)), kEps);
-        const double x = sqrt((double)gamma * pp / fmax(r0, 1e-14)) + sqrt(uu * uu + vv * vv);
-        best = nan_max_b(best, x);
+        // Rie_prob_2d_rs.py:312-315 on the new state (primitives as con2primi
+        // writes them), in the state's precision; the maximum and dt are FP64
+        const T r0 = v[0];
+        const T rho = fmax(r0, T(kEps));
+        T uu, vv;
+        if constexpr (FAST) {
+          const T ir = qrcp<T, FAST>(rho);
+          uu = v[1] * ir;
+          vv = v[2] * ir;
+        } else {
+          uu = v[1] / rho;
+          vv = v[2] / rho;
+        }
+        const T pp = fmax((gamma - T(1.0)) * (v[3] - T(0.5) * rho * (uu * uu + vv * vv)), T(kEps));
+        const T x = sqrt(qdiv<T, FAST>(gamma * pp, fmax(r0, T(1e-14)))) + sqrt(uu * uu + vv * vv);
+        best = nan_max_b(best, (double)x);
       }
     }
     if (stage == 3) {

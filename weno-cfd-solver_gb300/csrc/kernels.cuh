@@ -469,23 +469,38 @@ __global__ void __launch_bounds__(256) k_cfl_max(CView<T> q, int64_t nx, int64_t
   const int64_t total = nx * ny;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e / ny + 3, j = e % ny + 3;
-    double uu, vv, pp;
-    const double r0 = (double)q.at(i, j, 0);
-    if constexpr (AOS) {
-      uu = (double)q.at(i, j, 5);
-      vv = (double)q.at(i, j, 6);
-      pp = (double)q.at(i, j, 7);
+    if constexpr (!AOS && std::is_same<T, float>::value) {
+      // FP32 state: the wave speed in FP32 (the state's own precision; the
+      // maximum and dt stay FP64), the positivity of the recovered density and
+      // pressure in FP64 without a divide: rho > 0 and E rho - |m|^2/2 > 0.
+      const float r0 = q.at(i, j, 0), m1 = q.at(i, j, 1), m2 = q.at(i, j, 2), E = q.at(i, j, 3);
+      const double rd = r0, m1d = m1, m2d = m2;
+      if (!(rd > 0.0) || !((double)E * rd - 0.5 * (m1d * m1d + m2d * m2d) > 0.0)) nonpos = true;
+      const float rho = fmaxf(r0, float(kEps));
+      const float ir = __fdividef(1.0f, rho);
+      const float uu = m1 * ir, vv = m2 * ir;
+      const float pp = fmaxf(((float)gamma - 1.0f) * (E - 0.5f * rho * (uu * uu + vv * vv)), float(kEps));
+      const float w = sqrtf(uu * uu + vv * vv) + sqrtf((float)gamma * pp * __fdividef(1.0f, fmaxf(r0, 1e-14f)));
+      best = nan_max(best, (double)w);
     } else {
-      const double rho = fmax(r0, kEps);
-      uu = (double)q.at(i, j, 1) / rho;
-      vv = (double)q.at(i, j, 2) / rho;
-      const double praw = ((double)gamma - 1.0) * ((double)q.at(i, j, 3) - 0.5 * rho * (uu * uu + vv * vv));
-      pp = fmax(praw, kEps);
-      if (!(r0 > 0.0) || !(praw > 0.0)) nonpos = true;
+      double uu, vv, pp;
+      const double r0 = (double)q.at(i, j, 0);
+      if constexpr (AOS) {
+        uu = (double)q.at(i, j, 5);
+        vv = (double)q.at(i, j, 6);
+        pp = (double)q.at(i, j, 7);
+      } else {
+        const double rho = fmax(r0, kEps);
+        uu = (double)q.at(i, j, 1) / rho;
+        vv = (double)q.at(i, j, 2) / rho;
+        const double praw = ((double)gamma - 1.0) * ((double)q.at(i, j, 3) - 0.5 * rho * (uu * uu + vv * vv));
+        pp = fmax(praw, kEps);
+        if (!(r0 > 0.0) || !(praw > 0.0)) nonpos = true;
+      }
+      const double speed = sqrt(uu * uu + vv * vv);
+      const double c = sqrt((double)gamma * pp / fmax(r0, 1e-14));
+      best = nan_max(best, c + speed);
     }
-    const double speed = sqrt(uu * uu + vv * vv);
-    const double c = sqrt((double)gamma * pp / fmax(r0, 1e-14));
-    best = nan_max(best, c + speed);
   }
   nonpos = __any_sync(0xffffffffu, nonpos);
   if (nonpos && (threadIdx.x & 31) == 0) atomicOr(&ctl->status, 2);
