@@ -214,13 +214,9 @@ __device__ __forceinline__ void weno_range(double& e0, double& e1, double& e2) {
 }
 
 // Non-linear weighting of three candidate values with linear weights d.
-// Exact: the reference's a_k = d_k/(eps+b_k)^2, w_k = a_k/sum.
-// FAST double: one divide via the common denominator prod_j (eps+b_j)^2,
-// the three (eps+b_k) brought into a safe range first (weno_range) -- the
-// products then neither overflow nor lose the dominant weight, whatever the
-// magnitude of the stencil values.
-// FAST float and df64: reciprocals, because the float exponent range would
-// underflow the products.
+// Exact: the reference's a_k = d_k/(eps+b_k)^2, w_k = a_k/sum.  FAST (float
+// and df64, whose float exponent range rules out products of fourth powers):
+// reciprocals.  FAST native double uses weno_nd instead.
 template <class T, bool FAST>
 __device__ __forceinline__ T weno_combine(T e0, T e1, T e2, T d0, T d1, T d2, T p0, T p1, T p2, T scale) {
   if constexpr (!FAST) {
@@ -231,14 +227,8 @@ __device__ __forceinline__ T weno_combine(T e0, T e1, T e2, T d0, T d1, T d2, T 
     const T w0 = a0 / sum, w1 = a1 / sum, w2 = a2 / sum;
     const T r = w0 * p0 + w1 * p1 + w2 * p2;
     return scale == T(1.0) ? r : r / scale;
-  } else if constexpr (is_native_f64<T>) {
-    weno_range(e0, e1, e2);
-    const T s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
-    const T c0 = d0 * (s1 * s2), c1 = d1 * (s0 * s2), c2 = d2 * (s0 * s1);
-    const T num = c0 * p0 + c1 * p1 + c2 * p2;
-    const T den = (c0 + c1 + c2) * scale;
-    return num / den;
   } else {
+    static_assert(!is_native_f64<T>, "FAST double takes the common-denominator form (weno_nd)");
     const T a0 = d0 * qrcp<T, FAST>(e0 * e0);
     const T a1 = d1 * qrcp<T, FAST>(e1 * e1);
     const T a2 = d2 * qrcp<T, FAST>(e2 * e2);
@@ -247,8 +237,11 @@ __device__ __forceinline__ T weno_combine(T e0, T e1, T e2, T d0, T d1, T d2, T 
   }
 }
 
-// FAST native double: numerator and denominator of weno_combine, so that a
-// caller can share one divide between two reconstructions.
+// FAST native double: the weights in a common-denominator form,
+// d_k prod_{j != k} (eps+b_j)^2, returned as numerator and denominator so that
+// a caller can share one divide between two reconstructions; the (eps+b_k)
+// are first brought into a safe range (weno_range), so the products neither
+// overflow nor lose the dominant weight whatever the magnitude of the values.
 __device__ __forceinline__ void weno_nd(double e0, double e1, double e2, double d0, double d1, double d2, double p0,
                                         double p1, double p2, double scale, double& num, double& den) {
   weno_range(e0, e1, e2);
@@ -473,27 +466,18 @@ __device__ __forceinline__ void roe_avg(const T ul[4], const T ur[4], T gamma, T
   }
 }
 
-// Left eigenvectors, weno.rs:76-107 (x) and weno.rs:136-167 (y).
-template <class T, bool FAST, bool Y>
-__device__ __forceinline__ void left_eig(T rho, T u, T v, T c, T gamma, T L[4][4], T ic_in, T irho_in) {
+// Left eigenvectors, weno.rs:76-107 (x) and weno.rs:136-167 (y), in the
+// reference's operation order (FAST callers use CharScalars / project_left).
+template <class T, bool Y>
+__device__ __forceinline__ void left_eig(T rho, T u, T v, T c, T gamma, T L[4][4]) {
   const T g1 = gamma - T(1.0);
   const T kin = T(0.5) * (u * u + v * v);
-  T inv_rc, inv_c2, a, b, irho;
   const T vn = Y ? v : u;
-  if constexpr (!FAST) {
-    const T rc = rho * c;
-    inv_rc = T(1.0) / rc;
-    inv_c2 = T(1.0) / (c * c);
-    a = g1 * kin / (T(2.0) * c * c);
-    b = vn / (T(2.0) * c);
-  } else {
-    const T ic = ic_in;
-    irho = irho_in;
-    inv_rc = ic * irho;
-    inv_c2 = ic * ic;
-    a = T(0.5) * (g1 * kin) * inv_c2;
-    b = T(0.5) * vn * ic;
-  }
+  const T rc = rho * c;
+  const T inv_rc = T(1.0) / rc;
+  const T inv_c2 = T(1.0) / (c * c);
+  const T a = g1 * kin / (T(2.0) * c * c);
+  const T b = vn / (T(2.0) * c);
   const T gu = -g1 * u * inv_c2 / T(2.0);
   const T gv = -g1 * v * inv_c2 / T(2.0);
   const T gg = g1 * inv_c2 / T(2.0);
@@ -503,19 +487,11 @@ __device__ __forceinline__ void left_eig(T rho, T u, T v, T c, T gamma, T L[4][4
   if constexpr (!Y) {
     L[0][1] = gu - hr; L[0][2] = gv; L[0][3] = gg;
     L[3][1] = gu + hr; L[3][2] = gv; L[3][3] = gg;
-    if constexpr (!FAST) {
-      L[2][0] = -v / rho; L[2][1] = T(0.0); L[2][2] = T(1.0) / rho; L[2][3] = T(0.0);
-    } else {
-      L[2][0] = -v * irho; L[2][1] = T(0.0); L[2][2] = irho; L[2][3] = T(0.0);
-    }
+    L[2][0] = -v / rho; L[2][1] = T(0.0); L[2][2] = T(1.0) / rho; L[2][3] = T(0.0);
   } else {
     L[0][1] = gu; L[0][2] = gv - hr; L[0][3] = gg;
     L[3][1] = gu; L[3][2] = gv + hr; L[3][3] = gg;
-    if constexpr (!FAST) {
-      L[2][0] = -u / rho; L[2][1] = T(1.0) / rho; L[2][2] = T(0.0); L[2][3] = T(0.0);
-    } else {
-      L[2][0] = -u * irho; L[2][1] = irho; L[2][2] = T(0.0); L[2][3] = T(0.0);
-    }
+    L[2][0] = -u / rho; L[2][1] = T(1.0) / rho; L[2][2] = T(0.0); L[2][3] = T(0.0);
   }
   L[1][0] = T(1.0) - g1 * kin * inv_c2;
   L[1][1] = g1 * u * inv_c2;
@@ -539,20 +515,16 @@ __device__ __forceinline__ void right_eig(T rho, T u, T v, T h, T c, T R[4][4]) 
   }
 }
 
-// weno.rs:197-205 mat4_vec4: exact mode accumulates every product from 0.0 in
-// column order (FAST callers use project_left / project_right instead).
-template <class T, bool FAST>
+// weno.rs:197-205 mat4_vec4: every product accumulated from 0.0 in column
+// order, as the reference does (FAST callers use project_left / project_right).
+template <class T>
 __device__ __forceinline__ void mat4_vec4(const T M[4][4], const T x[4], T out[4]) {
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
-    if constexpr (!FAST) {
-      T acc = T(0.0);
+    T acc = T(0.0);
 #pragma unroll
-      for (int c = 0; c < 4; ++c) acc = acc + M[r][c] * x[c];
-      out[r] = acc;
-    } else {
-      out[r] = M[r][0] * x[0] + M[r][1] * x[1] + M[r][2] * x[2] + M[r][3] * x[3];
-    }
+    for (int c = 0; c < 4; ++c) acc = acc + M[r][c] * x[c];
+    out[r] = acc;
   }
 }
 
@@ -669,9 +641,9 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
       project_right<T, Y>(k, chr, qr);
     } else {
       T Lm[4][4];
-      left_eig<T, FAST, Y>(rho_a, u_a, v_a, c_a, gamma, Lm, ic_a, irho_a);
+      left_eig<T, Y>(rho_a, u_a, v_a, c_a, gamma, Lm);
 #pragma unroll
-      for (int s = 0; s < 6; ++s) mat4_vec4<T, FAST>(Lm, c[s], w[s]);
+      for (int s = 0; s < 6; ++s) mat4_vec4<T>(Lm, c[s], w[s]);
 #pragma unroll
       for (int f = 0; f < 4; ++f) {
         chl[f] = weno5_left<T, FAST>(w[0][f], w[1][f], w[2][f], w[3][f], w[4][f], weps);
@@ -679,8 +651,8 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
       }
       T Rm[4][4];
       right_eig<T, Y>(rho_a, u_a, v_a, h_a, c_a, Rm);
-      mat4_vec4<T, FAST>(Rm, chl, ql);
-      mat4_vec4<T, FAST>(Rm, chr, qr);
+      mat4_vec4<T>(Rm, chl, ql);
+      mat4_vec4<T>(Rm, chr, qr);
     }
     pp_limit<T, FAST>(ql, c[2], gamma);
     pp_limit<T, FAST>(qr, c[3], gamma);
