@@ -98,3 +98,46 @@ def test_fast_tracks_exact_at_2048(wx):
         s.close()
     for k in range(4):
         assert rel_l1(out["fast"][3:-3, 3:-3, k], out["exact"][3:-3, 3:-3, k]) <= 1e-10
+
+
+@pytest.mark.parametrize("shape", [(16384, 1024), (1024, 16384)])
+def test_free_stream_long_grids(wx, shape):
+    """Strongly non-square grids of 16.8 M cells (long rows, then long columns):
+    a uniform state stays uniform in FP64 fast and FP32."""
+    nx, ny = shape
+    q = np.zeros((nx + 6, ny + 6, 8))
+    rho, u, v, p = 0.7, -0.3, 0.6, 1.4
+    q[..., 0], q[..., 1], q[..., 2] = rho, rho * u, rho * v
+    q[..., 3] = p / 0.4 + 0.5 * rho * (u * u + v * v)
+    q[..., 4], q[..., 5], q[..., 6], q[..., 7] = rho, u, v, p
+    for precision, tol in ((64, 1e-13), (32, 1e-6)):
+        s = wx.Solver(nx, ny, 1.0 / max(nx, ny), G, precision=precision, mode="fast", cons=False, force_hlle=True,
+                      cfl=0.45)
+        s.set_state(q)
+        s.run(2)
+        got = s.state()
+        assert s.info()[2] == 0
+        for k in range(4):
+            assert np.abs(got[..., k] - q[..., k]).max() <= tol * abs(q[0, 0, k])
+
+
+def test_large_solve_in_a_batch(wx, orc):
+    """A 4096 x 2048 solve next to a 64 x 64 one in an FP32 batch (TMA boxes over a
+    large tensor map) agrees with the single-grid FP32 solver to FP32 rounding."""
+    from states import quadrant
+    rng = np.random.default_rng(31)
+    big = orc.sync_primitives(orc.bc_transmissive(quadrant(rng, 4096, 2048)), G)
+    small = orc.sync_primitives(orc.bc_transmissive(quadrant(rng, 64, 64)), G)
+    kw = dict(cons=True, force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.5)
+    b = wx.Batch(wx.Batch.pool_cells([(4096, 2048), (64, 64)], 32), 2, precision=32, **kw)
+    sb = b.add(big, 1.0 / 4096, max_steps=3)
+    b.add(small, 1.0 / 64, max_steps=3)
+    b.run(3)
+    got = b.state(sb)
+    s = wx.Solver(4096, 2048, 1.0 / 4096, G, precision=32, **kw)
+    s.set_state(big)
+    s.run(3)
+    ref = s.state()
+    assert b.info(sb)["steps"] == 3 and b.info(sb)["status"] == 0
+    for k in range(4):
+        assert rel_l1(got[3:-3, 3:-3, k], ref[3:-3, 3:-3, k]) <= 1e-6
