@@ -336,13 +336,11 @@ __device__ __forceinline__ void weno5_lr_fast(T u0, T u1, T u2, T u3, T u4, T u5
 // smoothness indicators are shared (the reference recomputes identical values).
 // FAST Gauss-point pair from the centre value, the slopes h_k of the three
 // candidate polynomials and the (scaled) indicators f_k: native double in the
-// common-denominator form, float and df64 with reciprocals.
+// common-denominator form, float and df64 with reciprocals.  The candidates
+// are q2 +- S h_k, so each weighted value is q2 plus S times a weighted slope.
 template <class T>
 __device__ __forceinline__ void gq_weights(T q2, T h0, T h1, T h2, T f0, T f1, T f2, T& ra, T& rb) {
   const T S = T(kSqrt3_12);
-  const T a0 = h0 * S, a1 = h1 * S, a2 = h2 * S;
-  const T pa0 = q2 + a0, pa1 = q2 - a1, pa2 = q2 - a2;
-  const T pb0 = q2 - a0, pb1 = q2 + a1, pb2 = q2 + a2;
   if constexpr (is_native_f64<T>) {
     weno_range(f0, f1, f2);
     const double s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
@@ -351,15 +349,16 @@ __device__ __forceinline__ void gq_weights(T q2, T h0, T h1, T h2, T f0, T f1, T
     const double ca0 = (kGqA0 / kGqA1) * P0, ca1 = P1, ca2 = (kGqA2 / kGqA1) * P2;
     const double cb0 = (kGqA2 / kGqA1) * P0, cb2 = (kGqA0 / kGqA1) * P2;
     const double sa = ca0 + ca1 + ca2, sb = cb0 + ca1 + cb2;
-    const double inv = 1.0 / (sa * sb);
-    ra = (ca0 * pa0 + ca1 * pa1 + ca2 * pa2) * sb * inv;
-    rb = (cb0 * pb0 + ca1 * pb1 + cb2 * pb2) * sa * inv;
+    const double t = S * (1.0 / (sa * sb));
+    // point a: candidates (q2 + S h0, q2 - S h1, q2 - S h2); point b: the mirror
+    ra = (ca0 * h0 - ca1 * h1 - ca2 * h2) * (sb * t) + q2;
+    rb = (ca1 * h1 + cb2 * h2 - cb0 * h0) * (sa * t) + q2;
   } else {
     const T r0 = qrcp<T, true>(f0 * f0), r1 = qrcp<T, true>(f1 * f1), r2 = qrcp<T, true>(f2 * f2);
     const T ca0 = T(kGqA0 / kGqA1) * r0, ca1 = r1, ca2 = T(kGqA2 / kGqA1) * r2;
     const T cb0 = T(kGqA2 / kGqA1) * r0, cb2 = T(kGqA0 / kGqA1) * r2;
-    ra = qdiv<T, true>(ca0 * pa0 + ca1 * pa1 + ca2 * pa2, ca0 + ca1 + ca2);
-    rb = qdiv<T, true>(cb0 * pb0 + ca1 * pb1 + cb2 * pb2, cb0 + ca1 + cb2);
+    ra = qdiv<T, true>((ca0 * h0 - ca1 * h1 - ca2 * h2) * S, ca0 + ca1 + ca2) + q2;
+    rb = qdiv<T, true>((ca1 * h1 + cb2 * h2 - cb0 * h0) * S, cb0 + ca1 + cb2) + q2;
   }
 }
 
