@@ -332,6 +332,74 @@ def run_c3(args):
     return 0
 
 
+def run_c0(args):
+    """The reference's own CPU-runnable case, end to end: 256^2 four-quadrant,
+    component WENO5 (epsilon 1e-6) + HLLC (blend 1e4/1.1e4), CFL 0.5, 200 steps,
+    FP64.  The same 200 steps are timed on the device solver (exact arithmetic,
+    bit-identical to the oracle's run, and fast arithmetic; graph replay, state
+    resident) and through host buffers (state in, 200 steps, state out), and on
+    the host cores with the oracle."""
+    import torch
+    torch.cuda.set_device(0)
+    import weno_ext
+    from weno_ext import problems
+    from oracle import oracle
+    n, steps = 256, 200
+    q0 = problems.quadrant(n, n, seed=20261200)
+    kw = dict(cons=True, force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.5, weno_eps=1e-6)
+    runs = {}
+    final = {}
+    for mode in ("exact", "fast"):
+        s = weno_ext.Solver(n, n, 1.0 / n, GAMMA, mode=mode, **kw)
+        s.set_state(q0)
+        s.run(steps)  # warm-up run (graph capture), then the timed one from the same state
+        s.synchronize()
+        s.set_state(q0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s.stream)
+        s.run(steps)
+        e1.record(s.stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        t0 = time.perf_counter()
+        s.set_state(q0)
+        s.run(steps)
+        final[mode] = s.state()
+        wall = time.perf_counter() - t0
+        runs[f"fp64_{mode}"] = {"ms_per_step": ms / steps, "cell_updates_per_s": n * n * steps / (ms / 1e3),
+                                "e2e_s": wall, "e2e_cell_updates_per_s": n * n * steps / wall,
+                                "status": s.info()[2]}
+        s.close()
+    oracle.set_threads(0)
+    oracle.set_weno_eps(1e-6)
+    ref = q0.copy()
+    t0 = time.perf_counter()
+    try:
+        for _ in range(steps):
+            dt = 0.5 / n / oracle.cfl_cmax(ref, n, n, GAMMA)
+            oracle.rk3_step(ref, n, n, 1.0 / n, dt, GAMMA, False, (1e4, 1.1e4), True)
+    finally:
+        oracle.set_weno_eps(1e-12)
+    cpu_s = time.perf_counter() - t0
+    rel = {nm: v["rel_l1"] for nm, v in _l1_linf(final["fast"], ref).items()}
+    line = {
+        "metric": "200-step run of the 256^2 configuration (component WENO5 eps 1e-6 + HLLC, FP64)",
+        "config_name": "c0", "value": runs["fp64_exact"]["e2e_cell_updates_per_s"], "unit": UNIT, "n_gpus": 1,
+        "dtype": "f64", "data": "synthetic", "higher_is_better": True,
+        "config": {"workload": "four-quadrant Riemann 256x256, cons-WENO5 (eps 1e-6) + GQ + HLLC, CFL 0.5, "
+                               "200 steps", "seed": 20261200},
+        "runs": runs,
+        "exact_bit_identical_to_oracle": bool(np.array_equal(final["exact"], ref)),
+        "fast_rel_l1_vs_oracle": rel,
+        "cpu_oracle": {"seconds": cpu_s, "cell_updates_per_s": n * n * steps / cpu_s, "cores": os.cpu_count(),
+                       "kind": "port"},
+        "speedup_e2e_exact_vs_cpu": cpu_s / runs["fp64_exact"]["e2e_s"],
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_dropin(args):
     """The reference-facing functions themselves (the weno_ext boundary) at nx x ny:
     l_local_py on torch CUDA tensors (device-resident) and on numpy arrays (host
@@ -465,8 +533,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="headline", choices=["headline", "c1", "c2", "c3", "c4", "dropin"],
-                    help="headline: the 4096^2 FP64 step (default); c1: 2048^2 FP64/FP32 accuracy run; "
+    ap.add_argument("--config", default="headline", choices=["headline", "c0", "c1", "c2", "c3", "c4", "dropin"],
+                    help="headline: the 4096^2 FP64 step (default); c0: the 256^2 200-step run end to end; "
+                         "c1: 2048^2 FP64/FP32 accuracy run; "
                          "c2: oblique shock 4096x1024 FP32 vs FP64; c3: batched uneven solves; c4: serving stream; "
                          "dropin: the weno_ext functions themselves (l_local_py & co.)")
     ap.add_argument("--solves", type=int, default=512)
@@ -483,6 +552,8 @@ def main():
         return run_c4(args)
     if args.config == "dropin":
         return run_dropin(args)
+    if args.config == "c0":
+        return run_c0(args)
 
     import torch
     from weno_ext import replicas
