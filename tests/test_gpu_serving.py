@@ -80,3 +80,34 @@ def test_rankine_hugoniot_matches_the_reference_dmr_state():
     assert abs(rho - 8.0) < 1e-12 and abs(p - 116.5) < 1e-12
     # the speed behind the shock is the reference's 8.25 (unitest.py:194-197)
     assert abs(math.hypot(u, v) - 8.25) < 1e-12
+
+
+def test_cancel_active_and_waiting_requests(wx):
+    """A request cancelled while on the GPU is stopped at the end of its pool's chunk
+    and one cancelled while waiting is never admitted; both end CANCELLED, and the
+    others finish with results equal to their runs alone."""
+    from weno_ext import serving
+    reqs = [serving.Request(rid=k, arrival=0.0, nx=48, ny=40, kind="quadrant", precision=32, t_end=0.03, seed=k)
+            for k in range(5)]
+    budget = serving.footprint_bytes(48, 40, 32) * 2 + 4096  # two at a time: the rest wait
+    srv = serving.Server(2 * budget, fp64_share=0.5, max_solves=4, steps_per_iter=2, keep_results=True)
+    seen = {}
+
+    def on_iteration(it, now):
+        if it == 1:
+            active = [r.rid for r in srv.active[32].values()]
+            seen["active"] = active[0]
+            srv.cancel(active[0])
+            srv.cancel(4)  # still waiting: the pool holds two solves
+
+    srv.serve(reqs, realtime=False, on_iteration=on_iteration, max_wall=120)
+    srv.close()
+    stopped = reqs[seen["active"]]
+    assert stopped.status == serving.CANCELLED and 0 < stopped.steps and stopped.t < stopped.t_end
+    assert reqs[4].status == serving.CANCELLED and reqs[4].steps == 0 and math.isnan(reqs[4].admitted)
+    done = [r for r in reqs if r.rid not in (seen["active"], 4)]
+    assert all(r.status == 0 and abs(r.t - r.t_end) < 1e-9 for r in done)
+    summary = serving.summarize(reqs, 1.0)
+    assert summary["cancelled"] == 2 and summary["failed"] == 0
+    solo = _alone(wx, done[0])
+    assert np.array_equal(solo.result, done[0].result)

@@ -14,6 +14,8 @@
 #include <vector>
 
 #include "../../include/weno_gb300.h"
+#include <nvtx3/nvToolsExt.h>
+
 #include "df64.cuh"
 #include "errors.h"
 #include "launch_api.h"
@@ -426,14 +428,17 @@ cudaError_t enqueue_step_t(weno_solver* s, int* launches) {
     void* in;
     HostPlanes qs, qo;
   } stages[3] = {{s->q, Q, Q1}, {s->q1, Q1, Q2}, {s->q2, Q2, Q}};
+  static const char* const kStageName[3] = {"weno RK3 stage 1", "weno RK3 stage 2", "weno RK3 stage 3"};
   for (int k = 0; k < 3; ++k) {
-    if ((e = residual_pipeline<T, FAST>(state_view(s, stages[k].in), s->M, s->N, *s->layout, s->ws, s->gamma, s->dx,
-                                        s->force_hlle, s->jp_lo, s->jp_hi, s->cons, k + 1, nullptr, Q, stages[k].qs,
-                                        stages[k].qo, s->ctl, st, tm, s->weps)))
-      return e;
-    if ((e = tm(TC_BC, true))) return e;
-    if ((e = bc_state<T, FAST>(s, stages[k].qo.p))) return e;
-    if ((e = tm(TC_BC, false))) return e;
+    // host-side NVTX range around the stage's launches (visible to profilers when
+    // the step is enqueued directly; a captured graph carries no ranges)
+    nvtxRangePushA(kStageName[k]);
+    e = residual_pipeline<T, FAST>(state_view(s, stages[k].in), s->M, s->N, *s->layout, s->ws, s->gamma, s->dx,
+                                   s->force_hlle, s->jp_lo, s->jp_hi, s->cons, k + 1, nullptr, Q, stages[k].qs,
+                                   stages[k].qo, s->ctl, st, tm, s->weps);
+    if (!e && !(e = tm(TC_BC, true)) && !(e = bc_state<T, FAST>(s, stages[k].qo.p))) e = tm(TC_BC, false);
+    nvtxRangePop();
+    if (e) return e;
     nl += per_residual + 1;
   }
   if ((e = launch_step_end(s->ctl, st))) return e;

@@ -70,6 +70,9 @@ class Request:
         return gen(self.nx, self.ny, seed=self.seed), 1.0 / max(self.nx, self.ny), dict(bc="transmissive")
 
 
+CANCELLED = -1  # Request.status of a cancelled request (library status codes are >= 0)
+
+
 def footprint_bytes(nx, ny, precision):
     es = 4 if precision == 32 else 8
     ld = -(-ny // (16 // es)) * (16 // es)  # rows padded to 16 bytes
@@ -112,6 +115,14 @@ class Server:
             self.pools[64] = Batch(b64 // (3 * 4 * 8), max_solves, precision=64, mode="fast",
                                    tile_config=tile_config[1], **kw)
         self.active = {p: {} for p in self.pools}  # slot -> request
+        self.cancelled = set()  # request ids to drop (waiting) or stop (active)
+
+    def cancel(self, rid):
+        """Cancel request `rid`: dropped if it has not been admitted yet, otherwise
+        stopped at the end of its pool's current chunk of steps (its slot and memory
+        are freed then).  Its status becomes CANCELLED; the other requests are not
+        affected.  May be called from the on_iteration callback."""
+        self.cancelled.add(rid)
 
     def _admit(self, r, now):
         pool = self.pools.get(r.precision)
@@ -151,12 +162,16 @@ class Server:
             while pending and pending[0].arrival <= now:
                 r = pending.popleft()
                 waiting[r.precision].append(r)
+            for p in self.pools:
+                for r in [r for r in waiting[p] if r.rid in self.cancelled]:
+                    waiting[p].remove(r)
+                    r.finished, r.status = now, CANCELLED
             progressed = False
             for p, pool in self.pools.items():
                 ev = inflight[p]
                 if ev is not None and not ev.query():
                     continue
-                if ev is not None:
+                if ev is not None or any(r.rid in self.cancelled for r in self.active[p].values()):
                     self._retire(p, time.perf_counter() - t0)
                     inflight[p] = None
                 while waiting[p] and self._admit(waiting[p][0], time.perf_counter() - t0):
@@ -185,9 +200,10 @@ class Server:
         pool = self.pools[p]
         act, tt, nn = pool.poll()
         for slot, r in list(self.active[p].items()):
-            if not act[slot]:
+            if not act[slot] or r.rid in self.cancelled:
                 inf = pool.info(slot)
-                r.finished, r.steps, r.t, r.status = now, inf["steps"], inf["t"], inf["status"]
+                r.finished, r.steps, r.t = now, inf["steps"], inf["t"]
+                r.status = CANCELLED if (act[slot] and r.rid in self.cancelled) else inf["status"]
                 if self.keep_results:
                     r.result = pool.state(slot)
                 pool.remove(slot)
@@ -203,7 +219,8 @@ def summarize(requests, wall):
     cu = sum(r.cells * r.steps for r in requests)
     return {
         "requests": len(requests),
-        "failed": sum(1 for r in requests if r.status != 0),
+        "failed": sum(1 for r in requests if r.status not in (0, CANCELLED)),
+        "cancelled": sum(1 for r in requests if r.status == CANCELLED),
         "p50_s": float(np.percentile(tts, 50)) if len(tts) else None,
         "p99_s": float(np.percentile(tts, 99)) if len(tts) else None,
         "mean_s": float(tts.mean()) if len(tts) else None,
