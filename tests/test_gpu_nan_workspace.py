@@ -71,3 +71,41 @@ def test_reconstruct_and_riemann_with_nan_scratch(wx, orc, ydir, cons):
     fn = orc.hllc_hlle_y_rs_py if ydir else orc.hllc_hlle_x_rs_py
     ref = fn(*refs, G, 0.05, 0.4, False)
     assert np.array_equal(rout.cpu().numpy(), ref)
+
+
+def test_solver_and_batch_with_nan_filled_buffers(wx, orc, golden_drivers, monkeypatch):
+    """With WENO_DEBUG_NAN_FILL=1 the solver's state, stage and workspace buffers and
+    the batch pools start as NaN bit patterns: the exact runs still equal the oracle's
+    and the reference drivers' own runs bit for bit."""
+    monkeypatch.setenv("WENO_DEBUG_NAN_FILL", "1")
+    rng = np.random.default_rng(43)
+    n = 20
+    q0 = orc.bc_reflecting(quadrant(rng, n, n))
+    ref = q0.copy()
+    for _ in range(4):
+        dt = 0.45 * (1.0 / n) / orc.cfl_cmax(ref, n, n, G)
+        orc.rk3_step(ref, n, n, 1.0 / n, dt, G, False, (0.05, 0.4), False)
+    s = wx.Solver(n, n, 1.0 / n, G, mode="exact", cons=False, force_hlle=False, jp_cri=(0.05, 0.4), cfl=0.45)
+    s.set_state(q0)
+    s.run(4)
+    assert np.array_equal(s.state(), ref)
+    g = golden_drivers
+    d = wx.Solver(40, 10, 0.1, G, cons=True, force_hlle=True, jp_cri=(10000, 11000), cfl=0.1, bc="dmr",
+                  bound=int(g["dmr/bound"]))
+    d.set_state(g["dmr/q0"])
+    d.run(4, t_final=0.01)
+    assert np.array_equal(d.state(), g["dmr/q_final"])
+    # batch: two uneven solves, exact FP64, against the oracle's runs
+    qa = orc.sync_primitives(orc.bc_transmissive(quadrant(rng, 37, 21)), G)
+    qb = orc.sync_primitives(orc.bc_transmissive(quadrant(rng, 18, 45)), G)
+    b = wx.Batch(wx.Batch.pool_cells([(37, 21), (18, 45)], 64), 2, precision=64, mode="exact", cons=False,
+                 force_hlle=True, jp_cri=(0.2, 1.0), cfl=0.45)
+    sa = b.add(qa, 1.0 / 37, max_steps=3)
+    sb = b.add(qb, 1.0 / 45, max_steps=3)
+    b.run(3)
+    for slot, q, nx, ny in ((sa, qa, 37, 21), (sb, qb, 18, 45)):
+        r = q.copy()
+        for _ in range(3):
+            dt = 0.45 * (1.0 / max(nx, ny)) / orc.cfl_cmax(r, nx, ny, G)
+            orc.rk3_step(r, nx, ny, 1.0 / max(nx, ny), dt, G, True, (0.2, 1.0), False)
+        assert np.array_equal(b.state(slot)[3:-3, 3:-3, :4], r[3:-3, 3:-3, :4])

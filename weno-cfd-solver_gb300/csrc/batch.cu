@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -322,6 +323,14 @@ int weno_batch_create(weno_batch** out, int64_t pool_cells, int max_solves, int 
     return bfail(WENO_ERR_CUDA, "batch_create: cuTensorMapEncodeTiled is not available from the driver");
   }
   if ((e = cudaMalloc(&b->pool_base, 3 * (size_t)b->capacity * b->es))) return bail(e, "cudaMalloc(pool)");
+  {
+    // WENO_DEBUG_NAN_FILL=1: pools start as a NaN bit pattern, so a tile load or
+    // a store outside a solve's written cells shows up as NaN in its results.
+    const char* v = std::getenv("WENO_DEBUG_NAN_FILL");
+    if (v && v[0] && v[0] != '0' &&
+        (e = cudaMemsetAsync(b->pool_base, 0xFF, 3 * (size_t)b->capacity * b->es, b->stream)))
+      return bail(e, "cudaMemsetAsync(pool)");
+  }
   for (int k = 0; k < 3; ++k) b->pool[k] = static_cast<char*>(b->pool_base) + (size_t)k * b->capacity * b->es;
   if ((e = cudaMalloc(&b->d_tmaps, sizeof(CUtensorMap) * max_solves))) return bail(e, "cudaMalloc(tensor maps)");
   b->h_tmaps.assign(max_solves, CUtensorMap{});

@@ -3,6 +3,8 @@
 // SSP-RK3 solver.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
@@ -130,6 +132,11 @@ cudaError_t residual_dispatch(int mode, HostView u, int64_t m, int64_t n, const 
                                            none, none, nullptr, st);
   return residual_pipeline<double, false>(u, m, n, Lo, ws, gamma, dx, force_hlle, jp_lo, jp_hi, cons, 0, out, none,
                                           none, none, nullptr, st);
+}
+
+bool debug_nan_fill() {
+  const char* v = std::getenv("WENO_DEBUG_NAN_FILL");
+  return v && v[0] && v[0] != '0';
 }
 
 int check_mode(int mode) {
@@ -536,9 +543,14 @@ int weno_solver_create(weno_solver** out, int64_t nx, int64_t ny, double dx, dou
   s->ctl_host->t_final = -1.0;
   if ((e = cudaMemcpyAsync(s->ctl, s->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, s->stream)))
     return bail(e, "cudaMemcpyAsync(control)");
-  if ((e = cudaMemsetAsync(s->q, 0, state_bytes, s->stream))) return bail(e, "cudaMemsetAsync");
-  if ((e = cudaMemsetAsync(s->q1, 0, state_bytes, s->stream))) return bail(e, "cudaMemsetAsync");
-  if ((e = cudaMemsetAsync(s->q2, 0, state_bytes, s->stream))) return bail(e, "cudaMemsetAsync");
+  // WENO_DEBUG_NAN_FILL=1 fills the state, stage and workspace buffers with a
+  // NaN bit pattern instead of zeros, so that any read of data the step did not
+  // write (a missed ghost cell, a stale stage) shows up as NaN in the results.
+  const int fill = debug_nan_fill() ? 0xFF : 0;
+  if ((e = cudaMemsetAsync(s->q, fill, state_bytes, s->stream))) return bail(e, "cudaMemsetAsync");
+  if ((e = cudaMemsetAsync(s->q1, fill, state_bytes, s->stream))) return bail(e, "cudaMemsetAsync");
+  if ((e = cudaMemsetAsync(s->q2, fill, state_bytes, s->stream))) return bail(e, "cudaMemsetAsync");
+  if (fill && (e = cudaMemsetAsync(s->ws, fill, s->layout->total, s->stream))) return bail(e, "cudaMemsetAsync");
   if ((e = cudaStreamSynchronize(s->stream))) return bail(e, "cudaStreamSynchronize");
   *out = s;
   return WENO_OK;
