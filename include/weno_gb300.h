@@ -132,7 +132,10 @@ enum { WENO_BC_TRANSMISSIVE = 0, WENO_BC_DMR = 1 };
 typedef struct weno_solver weno_solver;
 
 /* weno_eps: the WENO5 smoothness epsilon (<= 0: the reference's 1e-12,
- * weno.rs:223 / utils.rs:3); the density and pressure floors stay 1e-12. */
+ * weno.rs:223 / utils.rs:3); the density and pressure floors stay 1e-12.
+ * Debugging aid: with the environment variable WENO_DEBUG_NAN_FILL=1 the
+ * solver's (and weno_batch_create's) internal buffers start as NaN bit
+ * patterns instead of zeros, so reads of data a step did not write show up. */
 int weno_solver_create(weno_solver** out, int64_t nx, int64_t ny, double dx, double gamma, int precision, int mode,
                        int cons, int force_hlle, double jp_lo, double jp_hi, double cfl, double weno_eps, int bc_kind,
                        int64_t bound, const double* post8, void* stream);
