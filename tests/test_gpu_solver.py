@@ -132,3 +132,29 @@ def test_characteristic_blow_up_reproduced(wx, orc):
     assert np.array_equal(np.isnan(got), np.isnan(ref))
     fin = ~np.isnan(ref)
     assert np.array_equal(got[fin], ref[fin])
+
+
+def test_pinned_host_buffers_match_pageable(wx, orc):
+    """set_state_host / get_state_host on page-locked host memory (the e2e path of
+    the benchmark) give the same bits as on pageable memory."""
+    import torch
+    from weno_ext import _lib
+    L = _lib.load()
+    nx, ny = 33, 38
+    q0 = orc.bc_transmissive(quadrant(np.random.default_rng(17), nx, ny))
+    res = []
+    for pinned in (False, True):
+        s = wx.Solver(nx, ny, 1 / ny, G, mode="exact", cons=False, force_hlle=True, cfl=0.45)
+        if pinned:
+            src = torch.from_numpy(q0.copy()).pin_memory()
+            dst = torch.full((nx + 6, ny + 6, 8), float("nan"), dtype=torch.float64).pin_memory()
+            _lib.check(L.weno_solver_set_state_host(s._h, src.data_ptr(), 8), "set_state_host")
+            s.run(3)
+            _lib.check(L.weno_solver_get_state_host(s._h, dst.data_ptr()), "get_state_host")
+            res.append(dst.numpy().copy())
+        else:
+            s.set_state(q0)
+            s.run(3)
+            res.append(s.state())
+    assert np.isfinite(res[1]).all()
+    assert np.array_equal(res[0], res[1])
