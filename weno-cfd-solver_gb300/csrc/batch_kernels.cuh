@@ -146,6 +146,31 @@ __device__ __forceinline__ T tile_sensor(const T* pbar, int R, int C, int fr, in
   return sensor_weight<T, FAST>(dpdx, dpdy, p, jp_lo, jp_hi);
 }
 
+// Both Gauss-point values of the four components of one face side: `p`
+// points at the first of five transverse values of component 0, `ks` is the
+// component stride and `ts` the transverse stride.  FAST float runs the
+// components as two packed pairs on the FP32x2 instructions.
+template <class T, bool FAST>
+__device__ __forceinline__ void tile_gq_side(const T* p, int ks, int ts, T weps, T a1[4], T a2[4]) {
+  if constexpr (FAST && is_f32<T>) {
+#pragma unroll
+    for (int k = 0; k < 4; k += 2) {
+      const T* u = p + k * ks;
+      const T* w = u + ks;
+      f32x2 ra, rb;
+      weno5_gq_pair<f32x2, true>(f32x2(u[0], w[0]), f32x2(u[ts], w[ts]), f32x2(u[2 * ts], w[2 * ts]),
+                                 f32x2(u[3 * ts], w[3 * ts]), f32x2(u[4 * ts], w[4 * ts]), ra, rb, f32x2(weps));
+      a1[k] = ra.v.x, a1[k + 1] = ra.v.y, a2[k] = rb.v.x, a2[k + 1] = rb.v.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const T* u = p + k * ks;
+      weno5_gq_pair<T, FAST>(u[0], u[ts], u[2 * ts], u[3 * ts], u[4 * ts], a1[k], a2[k], weps);
+    }
+  }
+}
+
 // Riemann solver of one tile face and its store into the face buffer F
 // (HLLE flux planes, or HLLC + HLLE + mean pressure for the sensor blend).
 template <class T, bool FAST, bool Y, bool BLEND>
@@ -281,22 +306,14 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
       T ql[4], qr[4], fl[4], fr_[4];
       {
         T a1[4], a2[4], f1[4], f2[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const T* p = P1 + k * G::P1 + fr * G::P1XC + fc;
-          weno5_gq_pair<T, FAST>(p[0], p[1], p[2], p[3], p[4], a1[k], a2[k], weps);
-        }
+        tile_gq_side<T, FAST>(P1 + fr * G::P1XC + fc, G::P1, 1, weps, a1, a2);
         euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           fl[k] = T(0.5) * (f1[k] + f2[k]);
           ql[k] = T(0.5) * (a1[k] + a2[k]);
         }
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const T* p = P1 + (4 + k) * G::P1 + fr * G::P1XC + fc;
-          weno5_gq_pair<T, FAST>(p[0], p[1], p[2], p[3], p[4], a1[k], a2[k], weps);
-        }
+        tile_gq_side<T, FAST>(P1 + 4 * G::P1 + fr * G::P1XC + fc, G::P1, 1, weps, a1, a2);
         euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -362,24 +379,14 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
       T ql[4], qr[4], fl[4], fr_[4];
       {
         T a1[4], a2[4], f1[4], f2[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const T* p = P1 + k * G::P1 + fr * G::P1YC + fc;
-          weno5_gq_pair<T, FAST>(p[0], p[G::P1YC], p[2 * G::P1YC], p[3 * G::P1YC], p[4 * G::P1YC], a1[k], a2[k],
-                                 weps);
-        }
+        tile_gq_side<T, FAST>(P1 + fr * G::P1YC + fc, G::P1, G::P1YC, weps, a1, a2);
         euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           fl[k] = T(0.5) * (f1[k] + f2[k]);
           ql[k] = T(0.5) * (a1[k] + a2[k]);
         }
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const T* p = P1 + (4 + k) * G::P1 + fr * G::P1YC + fc;
-          weno5_gq_pair<T, FAST>(p[0], p[G::P1YC], p[2 * G::P1YC], p[3 * G::P1YC], p[4 * G::P1YC], a1[k], a2[k],
-                                 weps);
-        }
+        tile_gq_side<T, FAST>(P1 + 4 * G::P1 + fr * G::P1YC + fc, G::P1, G::P1YC, weps, a1, a2);
         euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {

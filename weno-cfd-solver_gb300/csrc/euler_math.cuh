@@ -19,6 +19,7 @@
 #include <type_traits>
 
 #include "df64.cuh"
+#include "f32x2.cuh"
 
 #ifndef WENO_TU_NS
 #error "WENO_TU_NS names the translation unit's inline namespace (tu_exact or tu_fast)"
@@ -332,6 +333,23 @@ __device__ __forceinline__ void weno5_lr_fast(T u0, T u1, T u2, T u3, T u4, T u5
   }
 }
 
+// FAST float: the four fields' left/right reconstructions as two packed pairs
+// (fields 0,1 and 2,3) on the FP32x2 instructions.
+__device__ __forceinline__ void weno5_lr_fast_f32_pairs(const float c[6][4], float weps, float left[4],
+                                                        float right[4]) {
+#pragma unroll
+  for (int f = 0; f < 4; f += 2) {
+    f32x2 l, r;
+    weno5_lr_fast<f32x2>(f32x2(c[0][f], c[0][f + 1]), f32x2(c[1][f], c[1][f + 1]), f32x2(c[2][f], c[2][f + 1]),
+                         f32x2(c[3][f], c[3][f + 1]), f32x2(c[4][f], c[4][f + 1]), f32x2(c[5][f], c[5][f + 1]),
+                         f32x2(weps), l, r);
+    left[f] = l.v.x;
+    left[f + 1] = l.v.y;
+    right[f] = r.v.x;
+    right[f + 1] = r.v.y;
+  }
+}
+
 // weno.rs:262-303: both Gauss-point values from one 5-cell stencil.  The
 // smoothness indicators are shared (the reference recomputes identical values).
 // FAST Gauss-point pair from the centre value, the slopes h_k of the three
@@ -601,7 +619,9 @@ __device__ __forceinline__ void pp_limit(T q[4], const T ub[4], T gamma) {
 // ---------------------------------------------------------------------------
 template <class T, bool FAST, bool Y, bool CHAR>
 __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T qr[4], T weps) {
-  if constexpr (!CHAR) {
+  if constexpr (!CHAR && FAST && is_f32<T>) {
+    weno5_lr_fast_f32_pairs(c, weps, ql, qr);
+  } else if constexpr (!CHAR) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       if constexpr (FAST) {
@@ -634,8 +654,13 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
       k.hr = T(0.5) * (ic_a * irho_a);
 #pragma unroll
       for (int s = 0; s < 6; ++s) project_left<T, Y>(k, c[s], w[s]);
+      if constexpr (is_f32<T>) {
+        weno5_lr_fast_f32_pairs(w, weps, chl, chr);
+      } else {
 #pragma unroll
-      for (int f = 0; f < 4; ++f) weno5_lr_fast<T>(w[0][f], w[1][f], w[2][f], w[3][f], w[4][f], w[5][f], weps, chl[f], chr[f]);
+        for (int f = 0; f < 4; ++f)
+          weno5_lr_fast<T>(w[0][f], w[1][f], w[2][f], w[3][f], w[4][f], w[5][f], weps, chl[f], chr[f]);
+      }
       project_right<T, Y>(k, chl, ql);
       project_right<T, Y>(k, chr, qr);
     } else {

@@ -186,12 +186,28 @@ template <class T, bool Y>
 __device__ __forceinline__ void gq_side_two(const Planes<T>& P, int64_t row, int64_t col, T gamma, T weps, T qA[4],
                                             T fA[4], T qB[4], T fB[4]) {
   T a1A[4], a2A[4], a1B[4], a2B[4];
+  if constexpr (is_f32<T>) {
+    // components (0,1) and (2,3) as packed pairs on the FP32x2 instructions
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    T v[6];
+    for (int k = 0; k < 4; k += 2) {
+      f32x2 v[6];
 #pragma unroll
-    for (int t = 0; t < 6; ++t) v[t] = Y ? P.at(k, row + 1 + t, col) : P.at(k, row, col + 1 + t);
-    weno5_gq_two<T>(v[0], v[1], v[2], v[3], v[4], v[5], weps, a1A[k], a2A[k], a1B[k], a2B[k]);
+      for (int t = 0; t < 6; ++t)
+        v[t] = Y ? f32x2(P.at(k, row + 1 + t, col), P.at(k + 1, row + 1 + t, col))
+                 : f32x2(P.at(k, row, col + 1 + t), P.at(k + 1, row, col + 1 + t));
+      f32x2 raA, rbA, raB, rbB;
+      weno5_gq_two<f32x2>(v[0], v[1], v[2], v[3], v[4], v[5], f32x2(weps), raA, rbA, raB, rbB);
+      a1A[k] = raA.v.x, a1A[k + 1] = raA.v.y, a2A[k] = rbA.v.x, a2A[k + 1] = rbA.v.y;
+      a1B[k] = raB.v.x, a1B[k + 1] = raB.v.y, a2B[k] = rbB.v.x, a2B[k + 1] = rbB.v.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      T v[6];
+#pragma unroll
+      for (int t = 0; t < 6; ++t) v[t] = Y ? P.at(k, row + 1 + t, col) : P.at(k, row, col + 1 + t);
+      weno5_gq_two<T>(v[0], v[1], v[2], v[3], v[4], v[5], weps, a1A[k], a2A[k], a1B[k], a2B[k]);
+    }
   }
   T f1[4], f2[4];
   euler_flux_pair<T, true, Y>(a1A, a2A, gamma, f1, f2);
