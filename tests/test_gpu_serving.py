@@ -74,14 +74,6 @@ def test_oversized_request_is_refused(wx):
     srv.close()
 
 
-def test_rankine_hugoniot_matches_the_reference_dmr_state():
-    from weno_ext import problems
-    rho, u, v, p = problems.rankine_hugoniot(10.0, math.pi / 3)
-    assert abs(rho - 8.0) < 1e-12 and abs(p - 116.5) < 1e-12
-    # the speed behind the shock is the reference's 8.25 (unitest.py:194-197)
-    assert abs(math.hypot(u, v) - 8.25) < 1e-12
-
-
 def test_cancel_active_and_waiting_requests(wx):
     """A request cancelled while on the GPU is stopped at the end of its pool's chunk
     and one cancelled while waiting is never admitted; both end CANCELLED, and the
