@@ -377,7 +377,7 @@ def run_c0(args):
     t0 = time.perf_counter()
     try:
         for _ in range(steps):
-            dt = 0.5 / n / oracle.cfl_cmax(ref, n, n, GAMMA)
+            dt = 0.5 * (1.0 / n) / oracle.cfl_cmax(ref, n, n, GAMMA)
             oracle.rk3_step(ref, n, n, 1.0 / n, dt, GAMMA, False, (1e4, 1.1e4), True)
     finally:
         oracle.set_weno_eps(1e-12)

@@ -22,7 +22,7 @@ def test_c0_full_run_matches_oracle(wx, orc):
     ref = q0.copy()
     try:
         for _ in range(steps):
-            dt = 0.5 / n / orc.cfl_cmax(ref, n, n, G)
+            dt = 0.5 * (1.0 / n) / orc.cfl_cmax(ref, n, n, G)
             orc.rk3_step(ref, n, n, 1.0 / n, dt, G, False, (1e4, 1.1e4), True)
     finally:
         orc.set_weno_eps(1e-12)
