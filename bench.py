@@ -141,9 +141,27 @@ def cpu_baseline(nx, strip_ny, threads, seconds_hint=15.0):
         if time.perf_counter() - t0 >= seconds_hint or steps >= 50:
             break
     el = time.perf_counter() - t0
-    return {"value": nx * strip_ny * steps / el, "unit": UNIT, "cores": used, "kind": "port",
+    line = {"value": nx * strip_ny * steps / el, "unit": UNIT, "cores": used, "kind": "port",
             "sample": f"{steps} SSP-RK3 step(s) of a {nx} x {strip_ny} strip of the same workload "
                       f"(oracle C++ restatement, OpenMP, {used} threads), {el:.1f} s"}
+    # The reference's Rust core is single-threaded: the same restatement on one core.
+    oracle.set_threads(1)
+    q1 = quadrant_state(nx, 4, seed=SEED + 1)
+    oracle.bc_transmissive(q1)
+    dt1 = 0.45 * dx / oracle.cfl_cmax(q1, nx, 4, GAMMA)
+    t0 = time.perf_counter()
+    steps1 = 0
+    while True:
+        oracle.rk3_step(q1, nx, 4, dx, dt1, GAMMA, True, (0.2, 1.0), False)
+        steps1 += 1
+        if time.perf_counter() - t0 >= seconds_hint / 5 or steps1 >= 40:
+            break
+    el1 = time.perf_counter() - t0
+    oracle.set_threads(used)
+    line["single_core"] = {"value": nx * 4 * steps1 / el1, "unit": UNIT, "cores": 1,
+                           "sample": f"{steps1} step(s) of a {nx} x 4 strip, one thread (the reference's Rust "
+                                     f"core is single-threaded), {el1:.1f} s"}
+    return line
 
 
 def run_reference(args):
@@ -382,6 +400,20 @@ def run_c0(args):
     finally:
         oracle.set_weno_eps(1e-12)
     cpu_s = time.perf_counter() - t0
+    # one core (the reference's Rust core is single-threaded): the first 20 steps
+    prev_threads = oracle.set_threads(0)
+    oracle.set_threads(1)
+    oracle.set_weno_eps(1e-6)
+    r1 = q0.copy()
+    t0 = time.perf_counter()
+    try:
+        for _ in range(20):
+            dt = 0.5 * (1.0 / n) / oracle.cfl_cmax(r1, n, n, GAMMA)
+            oracle.rk3_step(r1, n, n, 1.0 / n, dt, GAMMA, False, (1e4, 1.1e4), True)
+    finally:
+        oracle.set_weno_eps(1e-12)
+        oracle.set_threads(prev_threads)
+    one_s = (time.perf_counter() - t0) * steps / 20
     rel = {nm: v["rel_l1"] for nm, v in _l1_linf(final["fast"], ref).items()}
     line = {
         "metric": "200-step run of the 256^2 configuration (component WENO5 eps 1e-6 + HLLC, FP64)",
@@ -394,7 +426,10 @@ def run_c0(args):
         "fast_rel_l1_vs_oracle": rel,
         "cpu_oracle": {"seconds": cpu_s, "cell_updates_per_s": n * n * steps / cpu_s, "cores": os.cpu_count(),
                        "kind": "port"},
+        "cpu_oracle_single_core": {"seconds_extrapolated": one_s, "cell_updates_per_s": n * n * steps / one_s,
+                                   "cores": 1, "sample": "first 20 of the 200 steps, extrapolated"},
         "speedup_e2e_exact_vs_cpu": cpu_s / runs["fp64_exact"]["e2e_s"],
+        "speedup_e2e_exact_vs_single_core": one_s / runs["fp64_exact"]["e2e_s"],
     }
     print(json.dumps(line))
     return 0
