@@ -99,7 +99,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
+        sm, smax, watts, reasons = [], [], [], set()
         names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -110,11 +110,16 @@ class ClockSampler:
                 smax.append(float(parts[2]))
             except ValueError:
                 continue
+            try:
+                watts.append(float(parts[3]))
+            except ValueError:
+                pass
             for nm, val in zip(names[1:], parts[5:9]):
                 if val.lower() in ("active", "1"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w": statistics.median(watts) if watts else None}
 
 
 def dist_setup():
@@ -565,7 +570,7 @@ def main():
     ap.add_argument("--precision", default="f64", choices=["f64", "df64", "f32"],
                     help="arithmetic of the headline solver (f64 = IEEE double, the default; df64 = double-float "
                          "pairs on the FP32 pipes; f32)")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--config", default="headline", choices=["headline", "c0", "c1", "c2", "c3", "c4", "dropin"],
@@ -685,15 +690,34 @@ def main():
     s2.run(1, graph=True)
     L.weno_solver_get_state_host(s2._h, hp)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    clocks_e2e = ClockSampler(torch.cuda.current_device())
+    clocks_e2e.start()
+    pc = time.perf_counter
+    split = np.zeros(3)
+    t0 = pc()
+    evs = []
     for _ in range(args.e2e_steps):
-        _lib.check(L.weno_solver_set_state_host(s2._h, hp, 8), "e2e set_state")
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ta = pc()
+        _lib.check(L.weno_solver_set_state_host(s2._h, hp, 8), "e2e set_state")  # returns after the upload
+        tb = pc()
+        ev[0].record(s2.stream)
         s2.run(1, graph=True)
-        _lib.check(L.weno_solver_get_state_host(s2._h, hp), "e2e get_state")
+        ev[1].record(s2.stream)
+        _lib.check(L.weno_solver_get_state_host(s2._h, hp), "e2e get_state")  # waits for the step and the download
+        ev[2].record(s2.stream)
+        tc = pc()
+        split += (tb - ta, tc - tb, tc - ta)
+        evs.append(ev)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = pc() - t0
+    dev_step = sum(ev[0].elapsed_time(ev[1]) for ev in evs) / len(evs)
+    clk_e2e = clocks_e2e.stop()
     e2e = {"value": nx * ny * args.e2e_steps * world / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": M * N * 8 * 8, "d2h_bytes_per_step": M * N * 8 * 8,
+           "ms_per_step": 1e3 * e2e_s / args.e2e_steps,
+           "ms_upload": 1e3 * split[0] / args.e2e_steps, "ms_step_and_download": 1e3 * split[1] / args.e2e_steps,
+           "ms_device_step": dev_step, "clocks": clk_e2e,
            "path": "weno_solver_set_state_host -> run(1) -> weno_solver_get_state_host, pinned host buffer"}
     s2.close()
 

@@ -229,6 +229,12 @@ int weno_init_oblique_shock(double* out, int64_t nx, int64_t ny, double lx, doub
  * denominators, with no counterpart in the reference. */
 int weno_probe_rates(double* fp64_tflops, double* fp64_div_per_s, double* fp32_tflops, void* stream);
 
+/* Diagnostics: the FAST-mode FP64 reciprocal, reciprocal square root and
+ * square root (an FP32 hardware seed and one third-order Newton step; within
+ * 1, 1 and 2 ulp) of n device doubles x, written to the device array out as
+ * [1/x | 1/sqrt(x) | sqrt(x)] (3n doubles), for tests of their error bounds. */
+int weno_fast_math_eval(const double* x, double* out, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

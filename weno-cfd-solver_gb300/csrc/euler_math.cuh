@@ -20,6 +20,7 @@
 
 #include "df64.cuh"
 #include "f32x2.cuh"
+#include "fp64_fast.cuh"
 
 #ifndef WENO_TU_NS
 #error "WENO_TU_NS names the translation unit's inline namespace (tu_exact or tu_fast)"
@@ -56,23 +57,32 @@ __device__ __forceinline__ T vmax(T a, T b) { return fmax(a, b); }
 template <class T>
 __device__ __forceinline__ T vmin(T a, T b) { return fmin(a, b); }
 
-// a / b: the IEEE quotient except in FAST float, which uses the SFU path.
+// a / b: the IEEE quotient except in FAST float (the SFU path) and FAST double
+// (a times the three-FMA reciprocal of fp64_fast.cuh).
 template <class T, bool FAST>
 __device__ __forceinline__ T qdiv(T a, T b) {
   if constexpr (FAST && is_f32<T>) return __fdividef(a, b);
+  else if constexpr (FAST && is_native_f64<T>) return a * f64fast::rcp(b);
   else return a / b;
 }
 template <class T, bool FAST>
 __device__ __forceinline__ T qrcp(T b) {
   if constexpr (FAST && is_f32<T>) return __fdividef(1.0f, b);
+  else if constexpr (FAST && is_native_f64<T>) return f64fast::rcp(b);
   else return T(1.0) / b;
 }
+template <class T, bool FAST>
+__device__ __forceinline__ T qsqrt(T x) {
+  if constexpr (FAST && is_native_f64<T>) return f64fast::sqrt(x);
+  else return sqrt(x);
+}
 // 1/sqrt(x) of the FAST forms (x > 0): one reciprocal square root gives sqrt(x)
-// = x * r and 1/x = r * r, replacing a square root and two divisions.  CUDA's
-// double and float rsqrt (within 1 and 2 ulp); df64 takes 1/sqrt.
+// = x * r and 1/x = r * r, replacing a square root and two divisions.  Double:
+// fp64_fast.cuh (within 1 ulp); float: CUDA's rsqrtf (within 2 ulp); df64
+// takes 1/sqrt.
 template <class T>
 __device__ __forceinline__ T frsqrt(T x) {
-  if constexpr (is_native_f64<T>) return rsqrt(x);
+  if constexpr (is_native_f64<T>) return f64fast::rsqrt(x);
   else if constexpr (is_f32<T>) return rsqrtf(x);
   else return T(1.0) / sqrt(x);
 }
@@ -80,6 +90,15 @@ __device__ __forceinline__ T frsqrt(T x) {
 // ---------------------------------------------------------------------------
 // Conserved state helpers (utils.rs:9-35, utils.rs:74-109)
 // ---------------------------------------------------------------------------
+// The kinetic energy term 0.5 rho (u^2 + v^2) of a pressure, with u = m/rho and
+// v = n/rho for the (clamped) density rho: the reference's form, or in FAST the
+// same quantity as 0.5 (m u + n v) (rho u = m), two operations fewer.
+template <class T, bool FAST>
+__device__ __forceinline__ T half_rho_speed2(T rho, T m, T n, T u, T v) {
+  if constexpr (FAST) return T(0.5) * (m * u + n * v);
+  else return T(0.5) * rho * (u * u + v * v);
+}
+
 // Euler flux normal to x (Y = false) or y (Y = true), utils.rs:74-109.  `rinv`
 // (FAST only, when > 0) is 1/max(q[0], eps) computed by the caller.
 template <class T, bool FAST, bool Y>
@@ -94,7 +113,7 @@ __device__ __forceinline__ void euler_flux(const T q[4], T gamma, T f[4], T rinv
     u = q[1] / rho;
     v = q[2] / rho;
   }
-  const T p = (gamma - T(1.0)) * (q[3] - T(0.5) * rho * (u * u + v * v));
+  const T p = (gamma - T(1.0)) * (q[3] - half_rho_speed2<T, FAST>(rho, q[1], q[2], u, v));
   if constexpr (!Y) {
     f[0] = q[1];
     f[1] = q[1] * u + p;
@@ -118,12 +137,12 @@ __device__ __forceinline__ void euler_flux_pair(const T qa[4], const T qb[4], T 
     const T prod = ra * rb;
     T ia, ib;
     if (prod < T(1e300)) {
-      const T inv = T(1.0) / prod;
+      const T inv = f64fast::rcp(prod);
       ia = rb * inv;
       ib = ra * inv;
     } else {
-      ia = T(1.0) / ra;
-      ib = T(1.0) / rb;
+      ia = f64fast::rcp(ra);
+      ib = f64fast::rcp(rb);
     }
     euler_flux<T, FAST, Y>(qa, gamma, fa, ia);
     euler_flux<T, FAST, Y>(qb, gamma, fb, ib);
@@ -141,8 +160,8 @@ __device__ __forceinline__ void con2prim(T q0, T q1, T q2, T q3, T gamma, T& p, 
     const T r = qrcp<T, FAST>(rho);
     u = q1 * r;
     v = q2 * r;
-    p = vmax((gamma - T(1.0)) * (q3 - T(0.5) * rho * (u * u + v * v)), T(kEps));
-    a = sqrt(gamma * p * r);
+    p = vmax((gamma - T(1.0)) * (q3 - half_rho_speed2<T, FAST>(rho, q1, q2, u, v)), T(kEps));
+    a = qsqrt<T, FAST>(gamma * p * r);
     h = (q3 + p) * r;
   } else {
     u = q1 / rho;
@@ -167,7 +186,7 @@ __device__ __forceinline__ T clamped_pressure(const T q[4], T gamma) {
     u = q[1] / rho;
     v = q[2] / rho;
   }
-  return vmax((gamma - T(1.0)) * (q[3] - T(0.5) * rho * (u * u + v * v)), T(kEps));
+  return vmax((gamma - T(1.0)) * (q[3] - half_rho_speed2<T, FAST>(rho, q[1], q[2], u, v)), T(kEps));
 }
 
 // ---------------------------------------------------------------------------
@@ -197,14 +216,17 @@ __device__ __forceinline__ int max_biased_exp3(double a, double b, double c) {
   return max(ea, max(eb, ec));
 }
 
-// Brings (eps + beta_k) into the range where the fourth-power products of the
+// Brings (eps + beta_k) into the range where the products of the
 // common-denominator weights neither overflow nor lose the dominant weight.
-// For a largest value within [2^-200, 2^200] (every practical stencil) nothing
-// is done; otherwise all three are scaled by the same power of two that puts
-// the largest into [0.5, 1) (exact).  NaN and infinity pass through.
+// For a largest value within [2^-W, 2^W] (every practical stencil) nothing is
+// done; otherwise all three are scaled by the same power of two that puts the
+// largest into [0.5, 1) (exact).  NaN and infinity pass through.  W = 200 for
+// the fourth-power products of the WENO5 weights, 120 for the Gauss-point
+// pair, whose shared reciprocal takes an eighth-power product.
+template <int W = 200>
 __device__ __forceinline__ void weno_range(double& e0, double& e1, double& e2) {
   const int em = max_biased_exp3(e0, e1, e2);
-  if (em >= 1023 - 200 && em <= 1023 + 200) return;
+  if (em >= 1023 - W && em <= 1023 + W) return;
   if (em == 0x7ff || em == 0) return;
   int b = 2045 - em;
   if (b < 1) b = 1;
@@ -260,7 +282,7 @@ __device__ __forceinline__ void div_pair(double a, double b, double c, double d,
   const double bd = b * d;
   const int e = (__double2hiint(bd) >> 20) & 0x7ff;
   if (e > 64 && e < 1983) {
-    const double inv = 1.0 / (bd * k);
+    const double inv = f64fast::rcp(bd * k);
     x = a * d * inv;
     y = c * b * inv;
   } else {
@@ -360,17 +382,18 @@ template <class T>
 __device__ __forceinline__ void gq_weights(T q2, T h0, T h1, T h2, T f0, T f1, T f2, T& ra, T& rb) {
   const T S = T(kSqrt3_12);
   if constexpr (is_native_f64<T>) {
-    weno_range(f0, f1, f2);
+    weno_range<120>(f0, f1, f2);
     const double s0 = f0 * f0, s1 = f1 * f1, s2 = f2 * f2;
     const double P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
-    // linear weights divided by the centre one (a common factor)
-    const double ca0 = (kGqA0 / kGqA1) * P0, ca1 = P1, ca2 = (kGqA2 / kGqA1) * P2;
-    const double cb0 = (kGqA2 / kGqA1) * P0, cb2 = (kGqA0 / kGqA1) * P2;
-    const double sa = ca0 + ca1 + ca2, sb = cb0 + ca1 + cb2;
-    const double t = S * (1.0 / (sa * sb));
+    // linear weights divided by the centre one (a common factor): point a
+    // weighs (r0 P0, P1, r2 P2), point b the mirror (r2 P0, P1, r0 P2)
+    constexpr double r0 = kGqA0 / kGqA1, r2 = kGqA2 / kGqA1;
+    const double u0 = P0 * h0, u1 = P1 * h1, u2 = P2 * h2;
+    const double sa = fma(r0, P0, fma(r2, P2, P1)), sb = fma(r2, P0, fma(r0, P2, P1));
+    const double t = S * f64fast::rcp(sa * sb);
     // point a: candidates (q2 + S h0, q2 - S h1, q2 - S h2); point b: the mirror
-    ra = (ca0 * h0 - ca1 * h1 - ca2 * h2) * (sb * t) + q2;
-    rb = (ca1 * h1 + cb2 * h2 - cb0 * h0) * (sa * t) + q2;
+    ra = fma(r0, u0, fma(-r2, u2, -u1)) * (sb * t) + q2;
+    rb = fma(r0, u2, fma(-r2, u0, u1)) * (sa * t) + q2;
   } else {
     const T r0 = qrcp<T, true>(f0 * f0), r1 = qrcp<T, true>(f1 * f1), r2 = qrcp<T, true>(f2 * f2);
     const T ca0 = T(kGqA0 / kGqA1) * r0, ca1 = r1, ca2 = T(kGqA2 / kGqA1) * r2;
@@ -449,8 +472,8 @@ __device__ __forceinline__ void roe_avg(const T ul[4], const T ur[4], T gamma, T
     const T il = rl * rl, ir = rr * rr;
     const T u_l = ul[1] * il, v_l = ul[2] * il;
     const T u_r = ur[1] * ir, v_r = ur[2] * ir;
-    const T p_l = vmax((gamma - T(1.0)) * (ul[3] - T(0.5) * rho_l * (u_l * u_l + v_l * v_l)), T(kEps));
-    const T p_r = vmax((gamma - T(1.0)) * (ur[3] - T(0.5) * rho_r * (u_r * u_r + v_r * v_r)), T(kEps));
+    const T p_l = vmax((gamma - T(1.0)) * (ul[3] - half_rho_speed2<T, FAST>(rho_l, ul[1], ul[2], u_l, v_l)), T(kEps));
+    const T p_r = vmax((gamma - T(1.0)) * (ur[3] - half_rho_speed2<T, FAST>(rho_r, ur[1], ur[2], u_r, v_r)), T(kEps));
     const T id = qrcp<T, FAST>(sqrt_l + sqrt_r);
     u_roe = (ul[1] * rl + ur[1] * rr) * id;
     v_roe = (ul[2] * rl + ur[2] * rr) * id;
@@ -710,8 +733,8 @@ __device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], con
     r.u_r = qr[1] * ir; r.v_r = qr[2] * ir;
   }
   // FAST: sqrt(rho)*u = q1/sqrt(rho) and sqrt(rho)*h = (E+p)/sqrt(rho).
-  r.p_l = (gamma - T(1.0)) * (ql[3] - T(0.5) * r.ql0 * (r.u_l * r.u_l + r.v_l * r.v_l));
-  r.p_r = (gamma - T(1.0)) * (qr[3] - T(0.5) * r.qr0 * (r.u_r * r.u_r + r.v_r * r.v_r));
+  r.p_l = (gamma - T(1.0)) * (ql[3] - half_rho_speed2<T, FAST>(r.ql0, ql[1], ql[2], r.u_l, r.v_l));
+  r.p_r = (gamma - T(1.0)) * (qr[3] - half_rho_speed2<T, FAST>(r.qr0, qr[1], qr[2], r.u_r, r.v_r));
   r.p_l = vmax(r.p_l, T(kEps));
   r.p_r = vmax(r.p_r, T(kEps));
   if constexpr (!FAST) {
@@ -730,7 +753,7 @@ __device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], con
     h_t = ((ql[3] + r.p_l) * rsl + (qr[3] + r.p_r) * rsr) * id;
   }
   const T tmp = h_t - T(0.5) * (u_t * u_t + v_t * v_t);
-  const T a_t = sqrt(vmax((gamma - T(1.0)) * tmp, T(0.0)));
+  const T a_t = qsqrt<T, FAST>(vmax((gamma - T(1.0)) * tmp, T(0.0)));
   const T un_t = Y ? v_t : u_t;
   r.un_l = Y ? r.v_l : r.u_l;
   r.un_r = Y ? r.v_r : r.u_r;
@@ -817,7 +840,7 @@ __device__ __forceinline__ void hllc_flux(const RiemannPre<T, FAST, Y>& r, const
 // riemann.rs:394-405: blend weight from the normalised pressure gradient.
 template <class T, bool FAST>
 __device__ __forceinline__ T sensor_weight(T dpdx, T dpdy, T p, T jp_lo, T jp_hi) {
-  const T grad = sqrt(dpdx * dpdx + dpdy * dpdy);
+  const T grad = qsqrt<T, FAST>(dpdx * dpdx + dpdy * dpdy);
   const T jp = qdiv<T, FAST>(grad, vmax(p, T(kEps)));
   if (jp <= jp_lo) return T(1.0);
   if (jp >= jp_hi) return T(0.0);

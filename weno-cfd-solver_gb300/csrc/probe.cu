@@ -1,9 +1,12 @@
 // Live arithmetic-rate probe: the denominators of the compute roofline
 // (FP64 FMA, FP64 divide and FP32 FMA throughput of this GPU), measured with
-// CUDA events on independent FMA chains.
+// CUDA events on independent FMA chains; and an evaluator of the FAST FP64
+// reciprocal / square-root forms for their error-bound tests.
 #include <cuda_runtime.h>
+#include <cstdint>
 
 #include "../../include/weno_gb300.h"
+#include "fp64_fast.cuh"
 
 namespace {
 
@@ -23,6 +26,15 @@ __global__ void div_chains(double* out, int iters, double b) {
     x0 = b / x0 + 1.0; x1 = b / x1 + 1.0; x2 = b / x2 + 1.0; x3 = b / x3 + 1.0;
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3;
+}
+
+__global__ void k_fast_math(const double* x, double* out, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = x[i];
+  out[i] = weno::f64fast::rcp(v);
+  out[n + i] = weno::f64fast::rsqrt(v);
+  out[2 * n + i] = weno::f64fast::sqrt(v);
 }
 
 template <class F>
@@ -64,4 +76,14 @@ extern "C" int weno_probe_rates(double* fp64_tflops, double* fp64_div_per_s, dou
   if (!e && fp32_tflops) *fp32_tflops = 2.0 * 8 * it32 * lanes / (ms * 1e-3) / 1e12;
   cudaFree(buf);
   return e ? WENO_ERR_CUDA : WENO_OK;
+}
+
+extern "C" int weno_fast_math_eval(const double* x, double* out, int64_t n, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !out))) return WENO_ERR_ARG;
+  if (n == 0) return WENO_OK;
+  const int threads = 256;
+  const int64_t blocks = (n + threads - 1) / threads;
+  if (blocks > 0x7fffffff) return WENO_ERR_SHAPE;
+  k_fast_math<<<(unsigned)blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(x, out, n);
+  return cudaGetLastError() ? WENO_ERR_CUDA : WENO_OK;
 }

@@ -46,6 +46,7 @@ SIGNATURES = {
     "weno_solver_timing_report": (_i, [_vp, ctypes.POINTER(_d), ctypes.POINTER(_i64), _i]),
     "weno_solver_launches_per_step": (_i, [_vp]),
     "weno_probe_rates": (_i, [ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d), _vp]),
+    "weno_fast_math_eval": (_i, [_vp, _vp, _i64, _vp]),
     "weno_init_quadrant": (_i, [_vp, _i64, _i64, _i64, _i64, _vp, _d, _vp]),
     "weno_init_oblique_shock": (_i, [_vp, _i64, _i64, _d, _d, _d, _d, _d, _d, _d, _d, ctypes.POINTER(_i64), _vp,
                                      _vp]),
