@@ -129,7 +129,7 @@ def dist_setup():
     return world, rank, local
 
 
-def cpu_baseline(nx, strip_ny, threads, seconds_hint=15.0):
+def cpu_baseline(nx, strip_ny, threads, seconds_hint=10.0):
     """The oracle (C++ restatement of the Rust core and driver step) timed on host
     cores over a strip of the workload: nx x strip_ny interior cells."""
     from oracle import oracle
@@ -143,7 +143,7 @@ def cpu_baseline(nx, strip_ny, threads, seconds_hint=15.0):
     while True:
         oracle.rk3_step(q, nx, strip_ny, dx, dt, GAMMA, True, (0.2, 1.0), False)
         steps += 1
-        if time.perf_counter() - t0 >= seconds_hint or steps >= 50:
+        if time.perf_counter() - t0 >= seconds_hint or steps >= 400:
             break
     el = time.perf_counter() - t0
     line = {"value": nx * strip_ny * steps / el, "unit": UNIT, "cores": used, "kind": "port",
@@ -159,7 +159,7 @@ def cpu_baseline(nx, strip_ny, threads, seconds_hint=15.0):
     while True:
         oracle.rk3_step(q1, nx, 4, dx, dt1, GAMMA, True, (0.2, 1.0), False)
         steps1 += 1
-        if time.perf_counter() - t0 >= seconds_hint / 5 or steps1 >= 40:
+        if time.perf_counter() - t0 >= seconds_hint / 2 or steps1 >= 400:
             break
     el1 = time.perf_counter() - t0
     oracle.set_threads(used)
