@@ -59,6 +59,33 @@ __device__ __forceinline__ T vmax(T a, T b) { return fmax(a, b); }
 template <class T>
 __device__ __forceinline__ T vmin(T a, T b) { return fmin(a, b); }
 
+// Clamps and tests against a non-negative bound.  FAST native double reads the
+// operands' bits as signed 64-bit integers: for non-negative doubles that order
+// is the numeric order, and every value with the sign bit set (negatives, -0)
+// reads below any non-negative bound, so the result is max(x, c) / x < c for
+// every non-NaN x, on the integer pipe instead of an FP64 slot (GB300 issues
+// FP64 compares and min/max at the FP64 rate).  A NaN x with the sign bit clear
+// passes through where fmax would return the bound; NaN propagates through
+// the neighbouring arithmetic either way.  Used by the fluxes and the Riemann
+// solvers (pass 2); the pass-1 Roe average and limiter keep the FP64 forms,
+// with which the characteristic pass 1 compiles to 112 registers (4 CTAs per
+// SM), measured faster than the 92-register (5 CTA) build the integer forms give.
+template <class T, bool FAST>
+__device__ __forceinline__ T cmax(T x, T c) {
+  if constexpr (FAST && is_native_f64<T>) return __double_as_longlong(x) > __double_as_longlong(c) ? x : c;
+  else return vmax(x, c);
+}
+template <class T, bool FAST>
+__device__ __forceinline__ bool lt_bound(T x, T c) {
+  if constexpr (FAST && is_native_f64<T>) return __double_as_longlong(x) < __double_as_longlong(c);
+  else return x < c;
+}
+template <class T, bool FAST>
+__device__ __forceinline__ bool gt_zero(T x) {
+  if constexpr (FAST && is_native_f64<T>) return __double_as_longlong(x) > 0;
+  else return x > T(0.0);
+}
+
 // a / b: the IEEE quotient except in FAST float (the SFU path) and FAST double
 // (a times the three-FMA reciprocal of fp64_fast.cuh).
 template <class T, bool FAST>
@@ -105,10 +132,10 @@ __device__ __forceinline__ T half_rho_speed2(T rho, T m, T n, T u, T v) {
 // (FAST only, when > 0) is 1/max(q[0], eps) computed by the caller.
 template <class T, bool FAST, bool Y>
 __device__ __forceinline__ void euler_flux(const T q[4], T gamma, T f[4], T rinv = T(0.0)) {
-  const T rho = vmax(q[0], T(kEps));
+  const T rho = cmax<T, FAST>(q[0], T(kEps));
   T u, v;
   if constexpr (FAST) {
-    const T r = rinv > T(0.0) ? rinv : qrcp<T, FAST>(rho);
+    const T r = gt_zero<T, FAST>(rinv) ? rinv : qrcp<T, FAST>(rho);
     u = q[1] * r;
     v = q[2] * r;
   } else {
@@ -135,10 +162,10 @@ __device__ __forceinline__ void euler_flux(const T q[4], T gamma, T f[4], T rinv
 template <class T, bool FAST, bool Y>
 __device__ __forceinline__ void euler_flux_pair(const T qa[4], const T qb[4], T gamma, T fa[4], T fb[4]) {
   if constexpr (FAST && is_native_f64<T>) {
-    const T ra = vmax(qa[0], T(kEps)), rb = vmax(qb[0], T(kEps));
+    const T ra = cmax<T, FAST>(qa[0], T(kEps)), rb = cmax<T, FAST>(qb[0], T(kEps));
     const T prod = ra * rb;
     T ia, ib;
-    if (prod < T(1e300)) {
+    if (lt_bound<T, FAST>(prod, T(1e300))) {
       const T inv = f64fast::rcp(prod);
       ia = rb * inv;
       ib = ra * inv;
@@ -157,12 +184,12 @@ __device__ __forceinline__ void euler_flux_pair(const T qa[4], const T qb[4], T 
 // utils.rs:9-35 con2primi_local for one cell.
 template <class T, bool FAST>
 __device__ __forceinline__ void con2prim(T q0, T q1, T q2, T q3, T gamma, T& p, T& a, T& rho, T& u, T& v, T& h) {
-  rho = vmax(q0, T(kEps));
+  rho = cmax<T, FAST>(q0, T(kEps));
   if constexpr (FAST) {
     const T r = qrcp<T, FAST>(rho);
     u = q1 * r;
     v = q2 * r;
-    p = vmax((gamma - T(1.0)) * (q3 - half_rho_speed2<T, FAST>(rho, q1, q2, u, v)), T(kEps));
+    p = cmax<T, FAST>((gamma - T(1.0)) * (q3 - half_rho_speed2<T, FAST>(rho, q1, q2, u, v)), T(kEps));
     a = qsqrt<T, FAST>(gamma * p * r);
     h = (q3 + p) * r;
   } else {
@@ -178,7 +205,7 @@ __device__ __forceinline__ void con2prim(T q0, T q1, T q2, T q3, T gamma, T& p, 
 // shock sensor averages (riemann.rs:421-430).
 template <class T, bool FAST>
 __device__ __forceinline__ T clamped_pressure(const T q[4], T gamma) {
-  const T rho = vmax(q[0], T(kEps));
+  const T rho = cmax<T, FAST>(q[0], T(kEps));
   T u, v;
   if constexpr (FAST) {
     const T r = qrcp<T, FAST>(rho);
@@ -188,7 +215,7 @@ __device__ __forceinline__ T clamped_pressure(const T q[4], T gamma) {
     u = q[1] / rho;
     v = q[2] / rho;
   }
-  return vmax((gamma - T(1.0)) * (q[3] - half_rho_speed2<T, FAST>(rho, q[1], q[2], u, v)), T(kEps));
+  return cmax<T, FAST>((gamma - T(1.0)) * (q[3] - half_rho_speed2<T, FAST>(rho, q[1], q[2], u, v)), T(kEps));
 }
 
 // ---------------------------------------------------------------------------
@@ -720,8 +747,8 @@ struct RiemannPre {
 template <class T, bool FAST, bool Y>
 __device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], const T qr[4], T gamma) {
   RiemannPre<T, FAST, Y> r;
-  r.ql0 = vmax(ql[0], T(kEps));
-  r.qr0 = vmax(qr[0], T(kEps));
+  r.ql0 = cmax<T, FAST>(ql[0], T(kEps));
+  r.qr0 = cmax<T, FAST>(qr[0], T(kEps));
   T h_l, h_r, u_t, v_t, h_t;
   T rsl = T(0.0), rsr = T(0.0);  // FAST: 1/sqrt(rho) per side
   if constexpr (!FAST) {
@@ -737,8 +764,8 @@ __device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], con
   // FAST: sqrt(rho)*u = q1/sqrt(rho) and sqrt(rho)*h = (E+p)/sqrt(rho).
   r.p_l = (gamma - T(1.0)) * (ql[3] - half_rho_speed2<T, FAST>(r.ql0, ql[1], ql[2], r.u_l, r.v_l));
   r.p_r = (gamma - T(1.0)) * (qr[3] - half_rho_speed2<T, FAST>(r.qr0, qr[1], qr[2], r.u_r, r.v_r));
-  r.p_l = vmax(r.p_l, T(kEps));
-  r.p_r = vmax(r.p_r, T(kEps));
+  r.p_l = cmax<T, FAST>(r.p_l, T(kEps));
+  r.p_r = cmax<T, FAST>(r.p_r, T(kEps));
   if constexpr (!FAST) {
     const T srl = sqrt(r.ql0), srr = sqrt(r.qr0);
     const T denom_r = srl + srr;
@@ -755,7 +782,7 @@ __device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], con
     h_t = ((ql[3] + r.p_l) * rsl + (qr[3] + r.p_r) * rsr) * id;
   }
   const T tmp = h_t - T(0.5) * (u_t * u_t + v_t * v_t);
-  const T a_t = qsqrt<T, FAST>(vmax((gamma - T(1.0)) * tmp, T(0.0)));
+  const T a_t = qsqrt<T, FAST>(cmax<T, FAST>((gamma - T(1.0)) * tmp, T(0.0)));
   const T un_t = Y ? v_t : u_t;
   r.un_l = Y ? r.v_l : r.u_l;
   r.un_r = Y ? r.v_r : r.u_r;
@@ -764,9 +791,14 @@ __device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], con
   return r;
 }
 
-template <class T>
+template <class T, bool FAST>
 __device__ __forceinline__ T guard_denom(T d) {
-  if (fabs(d) < T(kEps)) d = copysign(T(kEps), d) + T(kEps);
+  bool small;
+  if constexpr (FAST && is_native_f64<T>)
+    small = (__double_as_longlong(d) & 0x7fffffffffffffffLL) < __double_as_longlong(kEps);
+  else
+    small = fabs(d) < T(kEps);
+  if (small) d = copysign(T(kEps), d) + T(kEps);
   return d;
 }
 
@@ -774,7 +806,7 @@ __device__ __forceinline__ T guard_denom(T d) {
 template <class T, bool FAST, bool Y>
 __device__ __forceinline__ void hlle_flux(const RiemannPre<T, FAST, Y>& r, const T ql[4], const T fl[4],
                                           const T qr[4], const T fr[4], T F[4]) {
-  const T denom = guard_denom(r.s_r - r.s_l);
+  const T denom = guard_denom<T, FAST>(r.s_r - r.s_l);
   if (r.s_l >= T(0.0)) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) F[k] = fl[k];
@@ -805,7 +837,7 @@ __device__ __forceinline__ void hllc_flux(const RiemannPre<T, FAST, Y>& r, const
     for (int k = 0; k < 4; ++k) F[k] = fl[k];
     return;
   }
-  const T denom = guard_denom(r.ql0 * (r.s_l - r.un_l) - r.qr0 * (r.s_r - r.un_r));
+  const T denom = guard_denom<T, FAST>(r.ql0 * (r.s_l - r.un_l) - r.qr0 * (r.s_r - r.un_r));
   const T s_star = qdiv<T, FAST>(
       r.p_r - r.p_l + r.ql0 * r.un_l * (r.s_l - r.un_l) - r.qr0 * r.un_r * (r.s_r - r.un_r), denom);
   if (r.s_l < T(0.0) && s_star >= T(0.0)) {
