@@ -1,9 +1,9 @@
 """Generate the golden vectors that pin the CPU oracle to the reference.
 
-Run in a checkout that has the reference sources (default location
-/root/reference, override with WENO_REFERENCE_DIR):
+Run with the path of a checkout of the reference sources in WENO_REFERENCE_DIR
+(there is no default location):
 
-    python tests/golden/make_golden.py
+    WENO_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 
 The reference's Rust extension cannot be built here (no Rust toolchain), so the
 vectors come from the reference's own Python code, imported unchanged:
@@ -33,7 +33,7 @@ import types
 
 import numpy as np
 
-REF = os.environ.get("WENO_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("WENO_REFERENCE_DIR", "")
 OUT = os.path.dirname(os.path.abspath(__file__))
 RUST_SQRT3_12 = 0.1443375673
 GAMMA = 1.4
@@ -53,6 +53,8 @@ def _install_stubs():
 
 
 def _import_reference():
+    if not REF or not os.path.isdir(REF):
+        sys.exit("set WENO_REFERENCE_DIR to a checkout of the reference (colinhu123/WENO-CFD-solver)")
     _install_stubs()
     sys.path.insert(0, REF)
     import WENO_HLLC_2d as twin  # noqa: E402
