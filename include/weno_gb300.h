@@ -207,6 +207,16 @@ int weno_batch_info(weno_batch* b, int slot, double* t, int64_t* steps, int* act
 /* Synchronise and copy every slot's active flag, time and step count (arrays of max_solves). */
 int weno_batch_poll(weno_batch* b, int* active, double* t, int64_t* steps);
 int weno_batch_stats(weno_batch* b, int64_t* ntiles, int64_t* free_cells, int* launches_per_step);
+/* Test hook of the bounded staging waits (no counterpart in the reference).
+ * From the next run on, the TMA copy of packed tile `tile` is not issued, so
+ * its wait gives up after wait_ns nanoseconds; the CTA then flags the solve of
+ * that tile and of every later tile it would have walked (status
+ * WENO_ERR_CUDA, and the solve stops at the end of the step) and leaves.  The
+ * tile list holds each added solve's tiles in slot order, rows then columns;
+ * grid > 0 fixes the stage kernels' persistent grid (CTA k walks tiles k,
+ * k + grid, ...).  tile < 0 restores normal operation (1 s waits, grid from
+ * occupancy).  No copy is left in flight and no GPU fault is involved. */
+int weno_batch_debug_skip_copy(weno_batch* b, int tile, int64_t wait_ns, int grid);
 
 /* ------------------------------------------------------------------------
  * Device generators of the seeded initial data, written straight into a
@@ -225,6 +235,22 @@ int weno_init_quadrant(double* out, int64_t nx, int64_t ny, int64_t si, int64_t 
 int weno_init_oblique_shock(double* out, int64_t nx, int64_t ny, double lx, double ly, double x0, double mach,
                             double theta, double rho1, double p1, double gamma, int64_t* bound_out, double* post8_out,
                             void* stream);
+
+/* Rie_prob_2d_rs.py:37-120 apply_bc_reflecting, in place on a device array
+ * (n, n, 8) in the drivers' layout: edge ghosts mirror the interior with the
+ * wall-normal momentum and velocity negated, then the four 3x3 corner blocks
+ * are taken from interior blocks with both pairs negated, as the reference
+ * does.  The reference indexes axis 0 with the axis-1 extent, so only square
+ * arrays (n >= 9) with 8 channels are accepted (WENO_ERR_SHAPE otherwise). */
+int weno_bc_reflecting(double* q, int64_t m, int64_t n, int64_t c, int64_t s0, int64_t s1, int64_t s2, void* stream);
+/* unitest.py:169-205 init_refac, the double-Mach set-up of
+ * double_mach_reflection.py, into a dense device array (nx+6, ny+6, 8): gas at
+ * rest (1.4, 0, 0, 1), the post-shock state (8, 4.125, -7.1447, 116.5) above
+ * the line y = sqrt(3) x - sqrt(3)/6 rounded to cell rows as the reference
+ * rounds them, then apply_bc_refac.  Returns the boundary's `bound` row; the
+ * inflow vector is the driver's literal (weno_solver_create with post8 NULL). */
+int weno_init_refac(double* out, int64_t nx, int64_t ny, double lx, double ly, double gamma, int64_t* bound_out,
+                    void* stream);
 
 /* Diagnostics: measured FP64 FMA (TFLOP/s), FP64 divide (per s) and FP32 FMA
  * (TFLOP/s) throughput of the current device -- the compute-roofline

@@ -6,6 +6,10 @@ ghost cells included (Rie_prob_2d_rs.py:213-263, unitest.py:169-205).
 
 * ``quadrant`` -- the four-quadrant Riemann problem with per-quadrant
   rho, p ~ U[0.1, 2] and u, v ~ U[-1, 1] (quadrant split at the middle).
+* ``reference_quadrant_device`` -- the reference driver's own four-quadrant
+  set-up (Rie_prob_2d_rs.init: fixed states, split at 3 + int(0.75 nx),
+  reflecting fill), and ``refac_device`` -- its double-Mach set-up
+  (unitest.init_refac), both generated on the device bit for bit.
 * ``oblique_shock`` -- a planar shock at angle ``theta`` to the lower wall,
   through (x0, 0), Mach ``mach`` into gas at rest (rho = 1.4, p = 1), post-shock
   state from the normal-shock Rankine-Hugoniot relations; lower wall with the
@@ -142,3 +146,50 @@ def oblique_shock_device(nx, ny, lx, ly, mach, theta, x0=1.0 / 6.0, gamma=GAMMA)
                                          float(theta), 1.4, 1.0, float(gamma), ctypes.byref(bound), post.ctypes.data,
                                          torch.cuda.current_stream().cuda_stream), "init_oblique_shock")
     return out, bound.value, post
+
+
+# Rie_prob_2d_rs.py:213-254 -- the reference's quadrant states (rho, u, v, p) in the
+# order (i < s, j < s), (i >= s, j < s), (i < s, j >= s), (i >= s, j >= s).
+REFERENCE_QUADRANTS = ((0.125, 1.0, 1.0, 0.025), (0.5, 0.0, 1.0, 0.25), (0.5, 1.0, 0.0, 0.25), (1.0, 0.0, 0.0, 1.0))
+
+
+def bc_reflecting_device(q):
+    """Rie_prob_2d_rs.apply_bc_reflecting in place on a square (n, n, 8) float64 CUDA tensor."""
+    import torch
+    from . import _lib
+    L = _lib.load()
+    if not (isinstance(q, torch.Tensor) and q.is_cuda and q.dtype == torch.float64 and q.dim() == 3):
+        raise TypeError("q: expected a 3-D float64 CUDA tensor")
+    s = q.stride()
+    _lib.check(L.weno_bc_reflecting(q.data_ptr(), *q.shape, *s, torch.cuda.current_stream().cuda_stream),
+               "bc_reflecting")
+    return q
+
+
+def reference_quadrant_device(n, gamma=GAMMA):
+    """Rie_prob_2d_rs.init on the current CUDA device: the (n+6, n+6, 8) array of the
+    reference's four-quadrant problem (square grids, as its reflecting fill requires)."""
+    import torch
+    from . import _lib
+    L = _lib.load()
+    out = torch.empty((n + 6, n + 6, 8), dtype=torch.float64, device="cuda")
+    si = 3 + int(n * 0.75)
+    prim = np.ascontiguousarray(np.array(REFERENCE_QUADRANTS, dtype=np.float64).reshape(16))
+    st = torch.cuda.current_stream().cuda_stream
+    _lib.check(L.weno_init_quadrant(out.data_ptr(), n, n, si, si, prim.ctypes.data, float(gamma), st),
+               "init_quadrant")
+    return bc_reflecting_device(out)
+
+
+def refac_device(nx, ny, lx=4.0, ly=1.0, gamma=GAMMA):
+    """unitest.init_refac on the current CUDA device: (tensor, bound) for
+    Solver(bc="dmr", bound=bound) with the driver's own inflow vector."""
+    import ctypes
+    import torch
+    from . import _lib
+    L = _lib.load()
+    out = torch.empty((nx + 6, ny + 6, 8), dtype=torch.float64, device="cuda")
+    bound = ctypes.c_int64()
+    _lib.check(L.weno_init_refac(out.data_ptr(), nx, ny, float(lx), float(ly), float(gamma), ctypes.byref(bound),
+                                 torch.cuda.current_stream().cuda_stream), "init_refac")
+    return out, bound.value
