@@ -142,3 +142,35 @@ def test_pool_cells_is_exact(wx, orc, precision):
     with pytest.raises(ValueError):
         for (nx, ny), q in zip(shapes, states):
             short.add(q, 1.0 / max(nx, ny))
+
+
+def test_staging_wait_runs_out(wx, orc):
+    """A staging copy that never lands (the test hook does not issue it) makes its bounded
+    wait give up: the CTA flags the solve of that tile and of every later tile it walks
+    (WENO_ERR_CUDA, stopped), and the other solves' results are those of a clean run.
+    Four solves on a fixed grid of 4 CTAs with 8 x 32 tiles: A (16 x 64) has tiles 0-3,
+    B, C and D (8 x 32) one tile each (4, 5, 6); CTA 0 walks tiles 0 and 4."""
+    rng = np.random.default_rng(41)
+    shapes = [(16, 64), (8, 32), (8, 32), (8, 32)]
+    qs = [synced(orc, quadrant(rng, nx, ny)) for nx, ny in shapes]
+    kw = dict(precision=32, mode="fast", cons=True, force_hlle=True, cfl=0.45, tile_config=0)
+
+    def batch():
+        b = wx.Batch(20000, 4, **kw)
+        return b, [b.add(q, 1.0 / max(nx, ny)) for q, (nx, ny) in zip(qs, shapes)]
+
+    clean, cs = batch()
+    clean.run(3)
+    hooked, hs = batch()
+    assert hooked.stats()["tiles"] == 7
+    hooked.debug_skip_copy(0, wait_ns=2_000_000, grid=4)
+    hooked.run(1)
+    hooked.debug_skip_copy(-1)
+    hooked.run(2)
+    st = [hooked.info(s) for s in hs]
+    assert [x["status"] for x in st] == [wx._lib.ERR_CUDA, wx._lib.ERR_CUDA, 0, 0]
+    assert not st[0]["active"] and not st[1]["active"]
+    assert st[0]["steps"] == 0 and st[1]["steps"] == 0
+    for k in (2, 3):
+        assert st[k]["steps"] == 3 and clean.info(cs[k])["status"] == 0
+        assert np.array_equal(hooked.state(hs[k]), clean.state(cs[k]))

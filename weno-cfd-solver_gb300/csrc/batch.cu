@@ -99,6 +99,11 @@ struct weno_batch {
   std::map<long long, long long> free_list;
   cudaGraphExec_t graph = nullptr;
   int graph_ntiles = -1;
+  // test hook (weno_batch_debug_skip_copy): tile whose staging copy is not issued,
+  // the bounded wait of every staging copy, and a fixed stage grid (0: occupancy)
+  int skip_tile = -1;
+  unsigned long long wait_ns = 1000000000ull;  // 1 s
+  int fixed_grid = 0;
 };
 
 namespace {
@@ -106,14 +111,15 @@ namespace {
 template <class T, bool FAST>
 cudaError_t enqueue_batch_step(weno_batch* b) {
   using BL = BatchLaunch<T, FAST>;
-  const int grid = std::min(b->ntiles, b->sm_count * b->occ);
+  const int grid = b->fixed_grid > 0 ? b->fixed_grid : std::min(b->ntiles, b->sm_count * b->occ);
   cudaError_t e;
   if ((e = BL::clock(b->d_ctl, b->max_solves, 0, b->stream))) return e;
   for (int s = 1; s <= 3; ++s) {
     // stage s reads pool s-1 (q, q1, q2) through the tensor maps
     void* qo = b->pool[s == 1 ? 1 : (s == 2 ? 2 : 0)];
     if ((e = BL::stage(b->cfg, b->chr, b->blend, b->d_solves, b->d_ctl, b->d_tiles, b->ntiles, grid, b->d_tmaps,
-                       b->pool[0], qo, s, b->gamma, b->jp_lo, b->jp_hi, b->weps, b->stream)))
+                       b->pool[0], qo, s, b->gamma, b->jp_lo, b->jp_hi, b->weps, b->skip_tile, b->wait_ns,
+                       b->stream)))
       return e;
   }
   return BL::clock(b->d_ctl, b->max_solves, 1, b->stream);
@@ -537,6 +543,17 @@ int weno_batch_poll(weno_batch* b, int* active, double* t, int64_t* steps) {
     if (t) t[s] = b->h_ctl[s].t;
     if (steps) steps[s] = b->h_ctl[s].steps;
   }
+  return WENO_OK;
+}
+
+int weno_batch_debug_skip_copy(weno_batch* b, int tile, int64_t wait_ns, int grid) {
+  if (!b) return bfail(WENO_ERR_ARG, "batch_debug_skip_copy: null handle");
+  if (tile >= 0 && (wait_ns <= 0 || grid < 0)) return bfail(WENO_ERR_ARG, "batch_debug_skip_copy: bad argument");
+  WB_CK(cudaStreamSynchronize(b->stream));
+  b->skip_tile = tile >= 0 ? tile : -1;
+  b->wait_ns = tile >= 0 ? (unsigned long long)wait_ns : 1000000000ull;
+  b->fixed_grid = tile >= 0 ? grid : 0;
+  b->graph_ntiles = -1;  // launch arguments changed: re-capture the step graph
   return WENO_OK;
 }
 

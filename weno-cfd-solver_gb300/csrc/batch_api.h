@@ -25,7 +25,8 @@ struct BatchLaunch {
   static int ctas_per_sm(int cfg, bool chr, bool blend);
   static cudaError_t stage(int cfg, bool chr, bool blend, const SolveDesc* solves, SolveCtl* ctl, const void* tiles,
                            int ntiles, int grid, const void* tmaps, const void* qn, void* qo, int stage, double gamma,
-                           double jp_lo, double jp_hi, double weps, cudaStream_t st);
+                           double jp_lo, double jp_hi, double weps, int skip_tile, unsigned long long wait_ns,
+                           cudaStream_t st);
   static cudaError_t cfl(int cfg, const SolveDesc* solves, SolveCtl* ctl, const void* tiles, int ntiles, int grid,
                          const void* q, double gamma, cudaStream_t st);
   static cudaError_t clock(SolveCtl* ctl, int nsolves, int phase, cudaStream_t st);

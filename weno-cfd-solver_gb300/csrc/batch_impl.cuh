@@ -19,19 +19,18 @@ constexpr size_t tile_smem() {
 template <class T, bool FAST, bool CHAR, bool BLEND, int TX, int TY>
 cudaError_t launch_stage(const SolveDesc* solves, SolveCtl* ctl, const int4* tiles, int ntiles, int grid,
                          const CUtensorMap* tmaps, const T* qn, T* qo, int stage, T gamma, T jp_lo, T jp_hi, T weps,
-                         cudaStream_t st) {
+                         int skip_tile, unsigned long long wait_ns, cudaStream_t st) {
   constexpr size_t sm = tile_smem<T, TX, TY, BLEND>();
   if constexpr (sm > 227 * 1024) {
     return cudaErrorInvalidConfiguration;
   } else {
     auto k = k_stage_tiles<T, FAST, CHAR, BLEND, TX, TY, kNT>;
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      if (e != cudaSuccess) return e;
-      attr_set = true;
-    }
-    k<<<grid, kNT, sm, st>>>(solves, ctl, tiles, ntiles, tmaps, qn, qo, stage, gamma, jp_lo, jp_hi, weps);
+    // The attribute is per device and cheap to set: set it on every launch (also
+    // keeps host threads from racing on a cached flag).
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k<<<grid, kNT, sm, st>>>(solves, ctl, tiles, ntiles, tmaps, qn, qo, stage, gamma, jp_lo, jp_hi, weps, skip_tile,
+                             wait_ns);
     return cudaGetLastError();
   }
 }
@@ -97,7 +96,7 @@ template <class T, bool FAST>
 cudaError_t BatchLaunch<T, FAST>::stage(int cfg, bool chr, bool blend, const SolveDesc* solves, SolveCtl* ctl,
                                         const void* tiles, int ntiles, int grid, const void* tmaps, const void* qn,
                                         void* qo, int stage, double gamma, double jp_lo, double jp_hi,
-                                        double weps, cudaStream_t st) {
+                                        double weps, int skip_tile, unsigned long long wait_ns, cudaStream_t st) {
   if (ntiles <= 0 || grid <= 0) return cudaSuccess;
   const int4* tl = static_cast<const int4*>(tiles);
   const CUtensorMap* a = static_cast<const CUtensorMap*>(tmaps);
@@ -107,16 +106,16 @@ cudaError_t BatchLaunch<T, FAST>::stage(int cfg, bool chr, bool blend, const Sol
 #define WENO_ST(TX, TY)                                                                                           \
   if (chr && blend)                                                                                               \
     e = bdetail::launch_stage<T, FAST, true, true, TX, TY>(solves, ctl, tl, ntiles, grid, a, b, o, stage, (T)gamma, \
-                                                           (T)jp_lo, (T)jp_hi, (T)weps, st);                               \
+                                                           (T)jp_lo, (T)jp_hi, (T)weps, skip_tile, wait_ns, st);                               \
   else if (chr)                                                                                                   \
     e = bdetail::launch_stage<T, FAST, true, false, TX, TY>(solves, ctl, tl, ntiles, grid, a, b, o, stage,         \
-                                                            (T)gamma, (T)jp_lo, (T)jp_hi, (T)weps, st);                    \
+                                                            (T)gamma, (T)jp_lo, (T)jp_hi, (T)weps, skip_tile, wait_ns, st);                    \
   else if (blend)                                                                                                 \
     e = bdetail::launch_stage<T, FAST, false, true, TX, TY>(solves, ctl, tl, ntiles, grid, a, b, o, stage,         \
-                                                            (T)gamma, (T)jp_lo, (T)jp_hi, (T)weps, st);                    \
+                                                            (T)gamma, (T)jp_lo, (T)jp_hi, (T)weps, skip_tile, wait_ns, st);                    \
   else                                                                                                            \
     e = bdetail::launch_stage<T, FAST, false, false, TX, TY>(solves, ctl, tl, ntiles, grid, a, b, o, stage,        \
-                                                             (T)gamma, (T)jp_lo, (T)jp_hi, (T)weps, st);
+                                                             (T)gamma, (T)jp_lo, (T)jp_hi, (T)weps, skip_tile, wait_ns, st);
   WENO_TILE_SWITCH(cfg, WENO_ST)
 #undef WENO_ST
   return e;

@@ -201,11 +201,11 @@ template <class T, bool FAST, bool CHAR, bool BLEND, int TX, int TY, int NT>
 __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict__ solves, SolveCtl* ctl,
                                                      const int4* __restrict__ tiles, int ntiles,
                                                      const CUtensorMap* tmaps, const T* Qn, T* Qo, int stage,
-                                                     T gamma, T jp_lo, T jp_hi, T weps) {
+                                                     T gamma, T jp_lo, T jp_hi, T weps, int skip_tile,
+                                                     unsigned long long wait_ns) {
   using G = TileGeom<TX, TY, BLEND>;
   static_assert(G::UC * sizeof(T) % 16 == 0, "box rows must be whole 16-byte units");
   constexpr uint32_t kBoxBytes = (uint32_t)(sizeof(T) * G::U_ELEMS);
-  constexpr uint64_t kWaitNs = 1000000000ull;  // 1 s
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* U = reinterpret_cast<T*>(smem_raw);
   T* P1 = U + G::U_ELEMS;
@@ -237,15 +237,20 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
       const CUtensorMap* tm = tmaps + tl.x;
       if (tid == 0) {
         tma::tensormap_acquire(tm);
-        tma::mbar_arrive_expect_tx(&bar, kBoxBytes);
-        tma::load_4d(U, tm, j0 - 4, i0 - HF - 3, 0, stage - 1, &bar);
+        if (t != skip_tile) {  // skip_tile >= 0 only under the test hook weno_batch_debug_skip_copy
+          tma::mbar_arrive_expect_tx(&bar, kBoxBytes);
+          tma::load_4d(U, tm, j0 - 4, i0 - HF - 3, 0, stage - 1, &bar);
+        }
       }
       const uint32_t par = phase;
       phase ^= 1u;
-      const bool landed = tma::mbar_wait_bounded(&bar, par, kWaitNs);
+      const bool landed = tma::mbar_wait_bounded(&bar, par, wait_ns);
       if (!__syncthreads_and(landed)) {
-        if (tid == 0) atomicOr(&ctl[tl.x].status, 4);
-        tma::mbar_wait_bounded(&bar, par, kWaitNs);  // let a late copy land before the CTA leaves
+        // This CTA leaves: flag the solve of this tile and of every later tile
+        // it would have walked, so no solve keeps stale tiles with a clean status.
+        if (tid == 0)
+          for (int t2 = t; t2 < ntiles; t2 += gridDim.x) atomicOr(&ctl[tiles[t2].x].status, 4);
+        tma::mbar_wait_bounded(&bar, par, wait_ns);  // let a late copy land before the CTA leaves
         return;
       }
     }
@@ -462,7 +467,8 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
           vv = v[2] / rho;
         }
         const T pp = fmax((gamma - T(1.0)) * (v[3] - T(0.5) * rho * (uu * uu + vv * vv)), T(kEps));
-        const T x = sqrt(qdiv<T, FAST>(gamma * pp, fmax(r0, T(1e-14)))) + sqrt(uu * uu + vv * vv);
+        const T rden = r0 != r0 ? r0 : fmax(r0, T(1e-14));  // np.maximum: a NaN density stays NaN
+        const T x = sqrt(qdiv<T, FAST>(gamma * pp, rden)) + sqrt(uu * uu + vv * vv);
         best = nan_max_b(best, (double)x);
       }
     }
@@ -504,7 +510,7 @@ __global__ void __launch_bounds__(NT) k_cfl_tiles(const SolveDesc* __restrict__ 
       const double rho = fmax(r0, kEps);
       const double uu = (double)Q[o + d.ps] / rho, vv = (double)Q[o + 2 * d.ps] / rho;
       const double pp = fmax(((double)gamma - 1.0) * ((double)Q[o + 3 * d.ps] - 0.5 * rho * (uu * uu + vv * vv)), kEps);
-      const double x = sqrt((double)gamma * pp / fmax(r0, 1e-14)) + sqrt(uu * uu + vv * vv);
+      const double x = sqrt((double)gamma * pp / (r0 != r0 ? r0 : fmax(r0, 1e-14))) + sqrt(uu * uu + vv * vv);
       best = nan_max_b(best, x);
     }
     for (int off = 16; off > 0; off >>= 1) best = nan_max_b(best, __shfl_xor_sync(0xffffffffu, best, off));
@@ -528,6 +534,11 @@ __global__ void k_solve_clock(SolveCtl* ctl, int nsolves, int phase) {
   if (s >= nsolves) return;
   SolveCtl& c = ctl[s];
   if (!c.active) return;
+  if (c.status & 4) {
+    // a tile of this solve was not staged in some stage: its state is incomplete
+    c.active = 0;
+    return;
+  }
   if (phase == 0) {
     const double cmax = __longlong_as_double((long long)c.cmax_bits) + 1e-16;
     if (!(cmax < INFINITY)) {

@@ -50,6 +50,8 @@ SIGNATURES = {
     "weno_init_quadrant": (_i, [_vp, _i64, _i64, _i64, _i64, _vp, _d, _vp]),
     "weno_init_oblique_shock": (_i, [_vp, _i64, _i64, _d, _d, _d, _d, _d, _d, _d, _d, ctypes.POINTER(_i64), _vp,
                                      _vp]),
+    "weno_bc_reflecting": (_i, [_vp, _i64, _i64, _i64, _i64, _i64, _i64, _vp]),
+    "weno_init_refac": (_i, [_vp, _i64, _i64, _d, _d, _d, ctypes.POINTER(_i64), _vp]),
     "weno_batch_tile_config_count": (_i, []),
     "weno_batch_create": (_i, [ctypes.POINTER(_vp), _i64, _i, _i, _i, _i, _i, _d, _d, _d, _d, _d, _i, _vp]),
     "weno_batch_destroy": (_i, [_vp]),
@@ -61,6 +63,7 @@ SIGNATURES = {
     "weno_batch_info": (_i, [_vp, _i, ctypes.POINTER(_d), ctypes.POINTER(_i64), ctypes.POINTER(_i),
                              ctypes.POINTER(_i)]),
     "weno_batch_poll": (_i, [_vp, _vp, _vp, _vp]),
+    "weno_batch_debug_skip_copy": (_i, [_vp, _i, _i64, _i]),
     "weno_batch_stats": (_i, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i)]),
 }
 

@@ -111,6 +111,12 @@ class Batch:
         _lib.check(self.L.weno_batch_stats(self._h, ctypes.byref(nt), ctypes.byref(fc), ctypes.byref(lp)), "stats")
         return {"tiles": nt.value, "free_cells": fc.value, "launches_per_step": lp.value}
 
+    def debug_skip_copy(self, tile, wait_ns=2_000_000, grid=0):
+        """Test hook of the bounded TMA waits: later runs do not issue the staging copy of
+        packed tile `tile` (its wait gives up after `wait_ns`); `grid` > 0 fixes the stage
+        kernels' persistent grid.  tile < 0 restores normal operation."""
+        _lib.check(self.L.weno_batch_debug_skip_copy(self._h, int(tile), int(wait_ns), int(grid)), "debug_skip_copy")
+
     def synchronize(self):
         self.stream.synchronize()
 
