@@ -18,8 +18,13 @@
 //
 // Host code cannot use the array's name as a device address, so the first call
 // on each device (with that device current) looks the address up with
-// cudaGetSymbolAddress and caches it.  That first call may load the module, so
-// it should happen before any stream capture.
+// cudaGetSymbolAddress and caches it together with the identity of the
+// device's current context.  A later call that finds another context (after
+// cudaDeviceReset, or a context torn down and created again in the same
+// process) looks the address up again instead of using the stale one.  That
+// first call may load the module, so it should happen before any stream
+// capture.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -37,6 +42,37 @@ static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 std::mutex g_mu;
 void* g_scratch_addr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};
+
+// The current context's unique id (cuCtxGetId), fetched through the runtime so
+// the library need not link the driver library; 0 if the driver lacks it, in
+// which case the address is looked up on every call.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  static CtxGetIdFn get_id = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetIdFn>(p);
+  }();
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 }  // namespace
 
@@ -55,10 +91,13 @@ extern "C" int weno_l_local_noalloc(const double* u, int64_t m, int64_t n, int64
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return weno::set_last_error(WENO_ERR_CUDA, cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return weno::set_last_error(WENO_ERR_ARG, "l_local_noalloc: device index too large");
+  // 0 when no context is current yet: the lookup below creates the device's
+  // primary context, and the id is read again after it.
+  const unsigned long long ctx = current_context_id();
   void* ptr = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_addr[dev]) {
+    if (!g_scratch_addr[dev] || ctx == 0 || g_scratch_ctx[dev] != ctx) {
       e = cudaGetSymbolAddress(&ptr, g_scratch);
       if (e != cudaSuccess) {
         char msg[256];
@@ -66,6 +105,7 @@ extern "C" int weno_l_local_noalloc(const double* u, int64_t m, int64_t n, int64
         return weno::set_last_error(WENO_ERR_CUDA, msg);
       }
       g_scratch_addr[dev] = ptr;
+      g_scratch_ctx[dev] = current_context_id();
     }
     ptr = g_scratch_addr[dev];
   }
