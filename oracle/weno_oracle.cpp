@@ -825,7 +825,9 @@ double orc_cfl_cmax(const double* q, int64_t M, int64_t N, int64_t C, int64_t nx
     for (int64_t j = 3; j < 3 + ny; ++j) {
       const double* c = q + (i * N + j) * C;
       double speed = std::sqrt(c[5] * c[5] + c[6] * c[6]);
-      double cs = std::sqrt(gamma * c[7] / std::fmax(c[0], 1e-14));
+      // np.maximum propagates NaN (a NaN density makes the wave speed NaN)
+      const double rden = c[0] != c[0] ? c[0] : std::fmax(c[0], 1e-14);
+      double cs = std::sqrt(gamma * c[7] / rden);
       double x = cs + speed;
       if (x != x) nan = true;
       if (x > cmax) cmax = x;

@@ -208,3 +208,55 @@ def test_errors(wx):
         wx.flux_x_py(np.ones((10, 10, 3)), G)
     with pytest.raises(ValueError):
         wx.hllc_hlle_x_rs_py(*[np.ones((1, 5, 4))] * 4, G, 0.1, 0.2, False)
+
+
+def _signed_nan(sign):
+    return np.array([0x7FF8000000000000 if sign > 0 else 0xFFF8000000000000], dtype=np.uint64).view(np.float64)[0]
+
+
+@pytest.mark.parametrize("sign", [1, -1], ids=["+nan", "-nan"])
+@pytest.mark.parametrize("cons", [False, True], ids=["char", "cons"])
+def test_nan_density_residual(wx, orc, sign, cons):
+    """A NaN density with either sign bit.  Exact mode reproduces the oracle bit for bit,
+    NaN positions included (the reference's f64::max clamps turn some NaN faces into finite
+    values).  FAST mode's integer-bit clamps let a NaN with the sign bit clear through where
+    f64::max returns the bound, so FAST outputs may hold NaN where exact ones are finite,
+    never the reverse on the characteristic path, where the projection spreads the NaN
+    to all four fields: there the NaN cell's residual is NaN in both modes."""
+    q = quadrant(np.random.default_rng(12), 24, 20)
+    q[14, 11, 0] = _signed_nan(sign)
+    ref = orc.l_local_py(q, 1.0 / 24, G, True, (0.2, 1.0), cons)
+    wx.set_mode("exact")
+    try:
+        got = wx.l_local_py(q, 1.0 / 24, G, True, (0.2, 1.0), cons)
+        check(got, ref, "exact", "l_local exact")
+        wx.set_mode("fast")
+        fast = wx.l_local_py(q, 1.0 / 24, G, True, (0.2, 1.0), cons)
+    finally:
+        wx.set_mode("exact")
+    if not cons:
+        assert np.isnan(ref[11, 8]).all() and np.isnan(fast[11, 8]).all()
+        assert not (np.isnan(ref) & ~np.isnan(fast)).any()
+    fin = np.isfinite(fast) & np.isfinite(ref)
+    far = np.ones(ref.shape[:2], dtype=bool)
+    far[11 - 4:11 + 5, 8 - 4:8 + 5] = False  # cells whose stencils reach the NaN cell
+    assert fin[far].all()
+    check(fast[far], ref[far], "fast", "l_local fast away from the NaN cell")
+
+
+@pytest.mark.parametrize("sign", [1, -1], ids=["+nan", "-nan"])
+@pytest.mark.parametrize("smode", ["exact", "fast"])
+def test_nan_density_stops_the_solver(wx, orc, sign, smode):
+    """The driver's CFL divides by np.maximum(rho, 1e-14), which is NaN for a NaN density,
+    so dt and the whole next state are NaN (Rie_prob_2d_rs.py:311-319).  The solver does
+    the same in both modes, and reports it (status bit 1, non-finite wave speed)."""
+    q = quadrant(np.random.default_rng(13), 24, 20)
+    q[14, 11, 0] = _signed_nan(sign)
+    assert np.isnan(orc.cfl_cmax(q, 24, 20, G))
+    s = wx.Solver(24, 20, 1.0 / 24, G, mode=smode, cons=False, force_hlle=True, cfl=0.45)
+    s.set_state(q)
+    s.run(1)
+    t, n, st = s.info()
+    assert st & 1
+    assert np.isnan(s.state()[3:-3, 3:-3, :4]).all()
+    s.close()

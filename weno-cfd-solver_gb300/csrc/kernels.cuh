@@ -472,6 +472,11 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* a, double 
   atomicMax(a, (unsigned long long)__double_as_longlong(x));
 }
 
+// np.maximum(rho, 1e-14) of the driver's CFL (Rie_prob_2d_rs.py:314): NaN in,
+// NaN out (fmax would return the bound).
+template <class T>
+__device__ __forceinline__ T np_maximum(T x, T c) { return x != x ? x : fmax(x, c); }
+
 // np.max propagates NaN (and inf dominates), so a non-finite wave speed makes
 // the maximum non-finite and dt follows, as in the driver; NaN's bit pattern
 // orders above +inf under the unsigned atomicMax.
@@ -496,7 +501,7 @@ __global__ void __launch_bounds__(256) k_cfl_max(CView<T> q, int64_t nx, int64_t
       const float ir = __fdividef(1.0f, rho);
       const float uu = m1 * ir, vv = m2 * ir;
       const float pp = fmaxf(((float)gamma - 1.0f) * (E - 0.5f * rho * (uu * uu + vv * vv)), float(kEps));
-      const float w = sqrtf(uu * uu + vv * vv) + sqrtf((float)gamma * pp * __fdividef(1.0f, fmaxf(r0, 1e-14f)));
+      const float w = sqrtf(uu * uu + vv * vv) + sqrtf((float)gamma * pp * __fdividef(1.0f, np_maximum(r0, 1e-14f)));
       best = nan_max(best, (double)w);
     } else {
       double uu, vv, pp;
@@ -514,7 +519,7 @@ __global__ void __launch_bounds__(256) k_cfl_max(CView<T> q, int64_t nx, int64_t
         if (!(r0 > 0.0) || !(praw > 0.0)) nonpos = true;
       }
       const double speed = sqrt(uu * uu + vv * vv);
-      const double c = sqrt((double)gamma * pp / fmax(r0, 1e-14));
+      const double c = sqrt((double)gamma * pp / np_maximum(r0, 1e-14));
       best = nan_max(best, c + speed);
     }
   }
