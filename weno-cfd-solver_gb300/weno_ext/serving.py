@@ -1,15 +1,25 @@
 """Serving loop: continuous batching of solve requests on one GPU.
 
 Requests arrive over time (a Poisson stream in the benchmark), each asking for
-one problem (grid, initial data, end time) at FP32 or FP64.  The server keeps
-one batched solver per precision, each with a fixed device pool carved from an
-HBM budget.  A request is admitted as soon as its footprint (3 RK buffers x 4
-conserved planes x its cells) fits in the free space of its pool and a slot is
-free; until then it waits in arrival order.  Every loop iteration advances all
-admitted solves of both pools by a few steps (the two pools run on their own
-streams and overlap on the device), then retires the solves that reached their
-end time, freeing their space for the next arrivals.  Time to solution is
-measured from arrival to retirement.
+one problem (grid, initial data, end time) at FP32 or FP64.  The HBM budget is
+divided into slabs; a slab holds one batched solver (weno_ext.Batch) of one
+precision, created when the slab is first needed.  A request is admitted as
+soon as its footprint (3 RK buffers x 4 conserved planes x its cells) fits in a
+slab of its precision, or in a free slab, which then takes that precision.
+Slabs follow the backlog: a slab whose solves have all retired is handed to
+the other precision when requests of that precision are waiting and fit
+nowhere, so the FP32/FP64 split is not fixed.
+
+Admission scans the waiting requests in arrival order and admits every one
+that fits (a large request at the head does not block smaller ones behind
+it).  An age bound keeps large requests from starving: once the oldest waiting
+request of a precision has waited longer than ``max_wait_s``, younger requests
+of that precision are held back until it is admitted.
+
+Each slab is driven on its own stream: when its last chunk of steps has
+finished (a CUDA event), its finished solves are retired, admission runs, and
+the next chunk is enqueued, so the slabs' work overlaps on the device.  Time to
+solution is measured from arrival to retirement.
 
 Each solve's arithmetic depends only on its own state (tiles and the per-solve
 dt reduction are independent of the other solves), so a result is bit-identical
@@ -96,97 +106,187 @@ def poisson_stream(n, rate, lo, hi, seed, fp64_fraction=0.25, t_end=(0.1, 0.3), 
     return reqs
 
 
+class _Slab:
+    __slots__ = ("index", "nbytes", "precision", "batch", "active", "inflight", "used", "draining")
+
+    def __init__(self, index, nbytes):
+        self.index = index
+        self.nbytes = nbytes
+        self.precision = None  # 32 or 64 once a batch lives here
+        self.batch = None
+        self.active = {}  # slot -> request
+        self.inflight = None  # CUDA event of the last enqueued chunk
+        self.used = 0  # footprint bytes of the admitted requests
+        self.draining = False  # takes no new requests: it is being emptied for the other precision
+
+    def fits(self, r):
+        return self.nbytes - self.used >= footprint_bytes(r.nx, r.ny, r.precision)
+
+
 class Server:
-    def __init__(self, hbm_budget_bytes, *, fp64_share=0.5, max_solves=1024, steps_per_iter=8, cfl=0.5,
-                 cons=True, force_hlle=False, jp_cri=(1e4, 1.1e4), tile_config=(1, 1), keep_results=False):
+    def __init__(self, hbm_budget_bytes, *, slabs=4, max_solves=1024, steps_per_iter=8, cfl=0.5, cons=True,
+                 force_hlle=False, jp_cri=(1e4, 1.1e4), tile_config=(1, 1), keep_results=False, max_wait_s=None,
+                 fp64_mode="fast"):
         import torch
         self.torch = torch
         self.steps_per_iter = int(steps_per_iter)
         self.keep_results = keep_results
-        b64 = int(hbm_budget_bytes * fp64_share)
-        b32 = int(hbm_budget_bytes) - b64
-        kw = dict(cons=cons, force_hlle=force_hlle, jp_cri=jp_cri, cfl=cfl)
-        self.pools = {}
-        self.budget = {32: b32, 64: b64}
-        if b32 > 0:
-            self.pools[32] = Batch(b32 // (3 * 4 * 4), max_solves, precision=32, mode="fast",
-                                   tile_config=tile_config[0], **kw)
-        if b64 > 0:
-            self.pools[64] = Batch(b64 // (3 * 4 * 8), max_solves, precision=64, mode="fast",
-                                   tile_config=tile_config[1], **kw)
-        self.active = {p: {} for p in self.pools}  # slot -> request
+        self.max_wait_s = max_wait_s
+        self.max_solves = int(max_solves)
+        self.fp64_mode = fp64_mode
+        self.tile_config = {32: tile_config[0], 64: tile_config[1]}
+        self.kw = dict(cons=cons, force_hlle=force_hlle, jp_cri=jp_cri, cfl=cfl)
+        n = max(1, int(slabs))
+        self.slab_bytes = int(hbm_budget_bytes) // n
+        self.slabs = [_Slab(k, self.slab_bytes) for k in range(n)]
         self.cancelled = set()  # request ids to drop (waiting) or stop (active)
+        self.conversions = 0  # slabs handed from one precision to the other
+
+    # -- views kept for callers of the two-pool layout -----------------------
+    @property
+    def active(self):
+        """{precision: {(slab, slot): request}} of the admitted requests."""
+        out = {32: {}, 64: {}}
+        for sl in self.slabs:
+            if sl.precision:
+                for slot, r in sl.active.items():
+                    out[sl.precision][(sl.index, slot)] = r
+        return out
+
+    @property
+    def pools(self):
+        """{precision: [Batch, ...]} of the slabs that hold a batch."""
+        out = {}
+        for sl in self.slabs:
+            if sl.batch is not None:
+                out.setdefault(sl.precision, []).append(sl.batch)
+        return out
 
     def cancel(self, rid):
         """Cancel request `rid`: dropped if it has not been admitted yet, otherwise
-        stopped at the end of its pool's current chunk of steps (its slot and memory
+        stopped at the end of its slab's current chunk of steps (its slot and memory
         are freed then).  Its status becomes CANCELLED; the other requests are not
         affected.  May be called from the on_iteration callback."""
         self.cancelled.add(rid)
 
-    def _admit(self, r, now):
-        pool = self.pools.get(r.precision)
-        if pool is None:
-            raise ValueError(f"no pool for precision {r.precision}")
+    # -- slabs ----------------------------------------------------------------
+    def _open(self, sl, precision):
+        es = 4 if precision == 32 else 8
+        mode = "fast" if precision == 32 else self.fp64_mode
+        sl.batch = Batch(sl.nbytes // (3 * 4 * es), self.max_solves, precision=precision, mode=mode,
+                         tile_config=self.tile_config[precision], **self.kw)
+        sl.precision = precision
+
+    def _release(self, sl):
+        sl.batch.close()
+        sl.batch = None
+        sl.precision = None
+        sl.active = {}
+        sl.inflight = None
+        sl.used = 0
+        sl.draining = False
+
+    def _try_add(self, sl, r, now):
         q, dx, bc = r.build()
         try:
-            r.slot = pool.add(q, dx, t_end=r.t_end, **bc)
+            r.slot = sl.batch.add(q, dx, t_end=r.t_end, **bc)
         except ValueError:
-            return False  # no space or no slot yet
+            return False  # no space (first-fit fragmentation) or no slot in this slab
         r.admitted = now
-        self.active[r.precision][r.slot] = r
+        sl.active[r.slot] = r
+        sl.used += footprint_bytes(r.nx, r.ny, r.precision)
         return True
+
+    def _place(self, r, now):
+        """Admit `r`: into an idle slab of its precision with room; if every slab of its
+        precision with room is busy, it waits for them (no new slab is opened); else into
+        a free slab, or into an idle, empty slab of the other precision, which changes
+        precision.  Returns "admitted", "busy" or "full"."""
+        mine = [sl for sl in self.slabs if sl.precision == r.precision and not sl.draining and sl.fits(r)]
+        for sl in mine:
+            if sl.inflight is None and self._try_add(sl, r, now):
+                return "admitted"
+        if any(sl.inflight is not None for sl in mine):
+            return "busy"
+        for sl in self.slabs:
+            if sl.precision is None:
+                self._open(sl, r.precision)
+                return "admitted" if self._try_add(sl, r, now) else "full"
+        for sl in self.slabs:
+            if sl.precision not in (None, r.precision) and not sl.active and sl.inflight is None:
+                self._release(sl)
+                self.conversions += 1
+                self._open(sl, r.precision)
+                return "admitted" if self._try_add(sl, r, now) else "full"
+        return "full"
+
+    def _admit_waiting(self, waiting, now):
+        held = set()  # precisions whose oldest request has waited past the age bound
+        for r in list(waiting):
+            if r.precision in held:
+                continue
+            res = self._place(r, now)
+            if res == "admitted":
+                waiting.remove(r)
+                continue
+            if self.max_wait_s is not None and now - r.arrival > self.max_wait_s:
+                held.add(r.precision)
+                if res == "full" and not any(sl.draining for sl in self.slabs):
+                    # no slab of its precision can take it: empty the other precision's
+                    # least-loaded slab so it can change hands
+                    other = [sl for sl in self.slabs if sl.precision not in (None, r.precision)]
+                    if other:
+                        min(other, key=lambda sl: sl.used).draining = True
 
     def serve(self, requests, realtime=True, on_iteration=None, max_wall=None):
         """Run the stream to completion; returns the requests with timings filled in.
 
-        Each pool is driven on its own: when its last chunk of steps has finished
-        (a CUDA event on its stream), its finished solves are retired, waiting
-        requests of its precision are admitted in arrival order, and the next chunk
-        is enqueued.  realtime=False skips idle time to the next arrival."""
+        A slab is serviced when its last chunk of steps has finished: its finished
+        solves are retired, waiting requests are admitted (every one that fits, in
+        arrival order, subject to the age bound), and its next chunk is enqueued.
+        realtime=False skips idle time to the next arrival."""
         torch = self.torch
         pending = deque(sorted(requests, key=lambda r: r.arrival))
-        waiting = {p: deque() for p in self.pools}
+        waiting = []
         for r in requests:
-            if r.precision not in self.pools:
-                raise ValueError(f"request {r.rid}: no pool for FP{r.precision}")
-            if footprint_bytes(r.nx, r.ny, r.precision) > self.budget.get(r.precision, 0):
-                raise ValueError(f"request {r.rid} ({r.nx}x{r.ny}, FP{r.precision}) exceeds its pool")
-        inflight = {p: None for p in self.pools}
+            if r.precision not in (32, 64):
+                raise ValueError(f"request {r.rid}: precision must be 32 or 64")
+            if footprint_bytes(r.nx, r.ny, r.precision) > self.slab_bytes:
+                raise ValueError(f"request {r.rid} ({r.nx}x{r.ny}, FP{r.precision}) exceeds a slab of "
+                                 f"{self.slab_bytes} bytes")
         t0 = time.perf_counter()
         iters = 0
-        while pending or any(waiting[p] for p in self.pools) or any(self.active[p] for p in self.pools):
+        while pending or waiting or any(sl.active for sl in self.slabs):
             now = time.perf_counter() - t0
             if max_wall is not None and now > max_wall:
                 raise TimeoutError("serving loop exceeded max_wall")
             while pending and pending[0].arrival <= now:
-                r = pending.popleft()
-                waiting[r.precision].append(r)
-            for p in self.pools:
-                for r in [r for r in waiting[p] if r.rid in self.cancelled]:
-                    waiting[p].remove(r)
-                    r.finished, r.status = now, CANCELLED
+                waiting.append(pending.popleft())
+            for r in [r for r in waiting if r.rid in self.cancelled]:
+                waiting.remove(r)
+                r.finished, r.status = now, CANCELLED
+            # retire on every slab whose chunk is done
+            for sl in self.slabs:
+                if sl.inflight is not None and sl.inflight.query():
+                    sl.inflight = None
+                    self._retire(sl, time.perf_counter() - t0)
+                elif sl.inflight is None and any(r.rid in self.cancelled for r in sl.active.values()):
+                    self._retire(sl, time.perf_counter() - t0)
+            if waiting:
+                self._admit_waiting(waiting, time.perf_counter() - t0)
             progressed = False
-            for p, pool in self.pools.items():
-                ev = inflight[p]
-                if ev is not None and not ev.query():
-                    continue
-                if ev is not None or any(r.rid in self.cancelled for r in self.active[p].values()):
-                    self._retire(p, time.perf_counter() - t0)
-                    inflight[p] = None
-                while waiting[p] and self._admit(waiting[p][0], time.perf_counter() - t0):
-                    waiting[p].popleft()
-                if self.active[p]:
-                    pool.run(self.steps_per_iter)
+            for sl in self.slabs:
+                if sl.inflight is None and sl.active:
+                    sl.batch.run(self.steps_per_iter)
                     ev = torch.cuda.Event()
-                    ev.record(pool.stream)
-                    inflight[p] = ev
+                    ev.record(sl.batch.stream)
+                    sl.inflight = ev
                     progressed = True
                     iters += 1
             if on_iteration and progressed:
                 on_iteration(iters, now)
-            if not any(inflight.values()):
-                if pending and not any(waiting[p] for p in self.pools):
+            if not any(sl.inflight is not None for sl in self.slabs):
+                if pending and not waiting:
                     wait = pending[0].arrival - (time.perf_counter() - t0)
                     if realtime:
                         time.sleep(max(0.0, min(wait, 0.01)))
@@ -196,10 +296,10 @@ class Server:
                 time.sleep(0.0002)
         return requests
 
-    def _retire(self, p, now):
-        pool = self.pools[p]
+    def _retire(self, sl, now):
+        pool = sl.batch
         act, tt, nn = pool.poll()
-        for slot, r in list(self.active[p].items()):
+        for slot, r in list(sl.active.items()):
             if not act[slot] or r.rid in self.cancelled:
                 inf = pool.info(slot)
                 r.finished, r.steps, r.t = now, inf["steps"], inf["t"]
@@ -207,16 +307,27 @@ class Server:
                 if self.keep_results:
                     r.result = pool.state(slot)
                 pool.remove(slot)
-                del self.active[p][slot]
+                del sl.active[slot]
+                sl.used -= footprint_bytes(r.nx, r.ny, r.precision)
 
     def close(self):
-        for b in self.pools.values():
-            b.close()
+        for sl in self.slabs:
+            if sl.batch is not None:
+                self._release(sl)
 
 
 def summarize(requests, wall):
     tts = np.array([r.finished - r.arrival for r in requests if r.status == 0])
     cu = sum(r.cells * r.steps for r in requests)
+    per = {}
+    for p in (32, 64):
+        t = np.array([r.finished - r.arrival for r in requests if r.status == 0 and r.precision == p])
+        w = np.array([r.admitted - r.arrival for r in requests if r.status == 0 and r.precision == p])
+        if len(t):
+            per[f"fp{p}"] = {"requests": int(len(t)), "p50_s": float(np.percentile(t, 50)),
+                             "p99_s": float(np.percentile(t, 99)), "p50_queue_s": float(np.percentile(w, 50)),
+                             "p99_queue_s": float(np.percentile(w, 99)),
+                             "cell_updates": int(sum(r.cells * r.steps for r in requests if r.precision == p))}
     return {
         "requests": len(requests),
         "failed": sum(1 for r in requests if r.status not in (0, CANCELLED)),
@@ -228,4 +339,5 @@ def summarize(requests, wall):
         "wall_s": wall,
         "aggregate_cell_updates_per_s": cu / wall if wall > 0 else None,
         "fp64_requests": sum(1 for r in requests if r.precision == 64),
+        "by_precision": per,
     }
