@@ -40,7 +40,7 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "weno-cfd-solver_gb300")
-for _p in (ROOT, PKG, os.path.join(ROOT, "tests")):
+for _p in (ROOT, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
@@ -53,8 +53,8 @@ CLASSES = ["cfl+dt", "bc", "pass1_x", "pass2_x", "blend", "pass1_y", "pass2_y", 
 
 
 def quadrant_state(nx, ny, seed=SEED):
-    from states import quadrant
-    return quadrant(np.random.default_rng(seed), nx, ny)
+    from weno_ext import problems
+    return problems.quadrant(nx, ny, seed=seed)
 
 
 def load_json(path):
@@ -218,140 +218,232 @@ def _l1_linf(a, b):
     return out
 
 
+def _lockstep(nx, ny, dx, q0, kw, runs, checkpoints):
+    """Run the solvers of `runs` [(name, precision, mode)] side by side from q0, timing
+    each on its own stream; returns per-run timings and, at every checkpoint, the
+    L1/Linf of each run against the first one."""
+    import torch
+    import weno_ext
+    sol = {}
+    for name, prec, mode in runs:
+        s = weno_ext.Solver(nx, ny, dx, GAMMA, precision=prec, mode=mode, **kw)
+        s.set_state(q0)
+        sol[name] = s
+    ms = {name: 0.0 for name in sol}
+    tot0 = {name: s.totals() for name, s in sol.items()}
+    errs, done = [], 0
+    ref = runs[0][0]
+    for c in checkpoints:
+        for name, s in sol.items():
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s.stream)
+            s.run(c - done)
+            e1.record(s.stream)
+            e1.synchronize()
+            ms[name] += e0.elapsed_time(e1)
+        done = c
+        st = {name: s.state() for name, s in sol.items()}
+        errs.append({"step": c, **{name: _l1_linf(st[name], st[ref]) for name in st if name != ref}})
+    res = {}
+    for name, s in sol.items():
+        t, k, status = s.info()
+        res[name] = {"steps": k, "t": t, "status": status, "ms_per_step": ms[name] / max(done, 1),
+                     "cell_updates_per_s": nx * ny * k / (ms[name] / 1e3) if ms[name] else None,
+                     "totals_start": tot0[name], "totals_end": s.totals()}
+        s.close()
+    return res, errs
+
+
+def _first_nonfinite(nx, ny, dx, q0, kw, nsteps, mode):
+    """First step after which the state holds a non-finite value (None if none within nsteps)."""
+    import weno_ext
+    s = weno_ext.Solver(nx, ny, dx, GAMMA, precision=64, mode=mode, **kw)
+    s.set_state(q0)
+    blow = None
+    for k in range(1, nsteps + 1):
+        s.run(1)
+        if not all(math.isfinite(x) for x in s.totals()):
+            blow = k
+            break
+    s.close()
+    return blow
+
+
 def run_accuracy(args):
-    """c1: 2048^2 four-quadrant, char-WENO5 + GQ + HLLE, CFL 0.45, 500 steps in FP64
-    exact (bit-identical to the reference arithmetic), FP64 fast and FP32; L1/Linf of
-    FP32 and fast against exact.  c2: oblique shock 4096x1024 on [0,4]x[0,1], seeded
-    Mach ~ U[2,10], angle ~ U[30,75] deg, char-WENO5 + HLLC (blend 1e4/1.1e4), CFL 0.1,
-    1000 steps, FP32 bulk (FP64 dt, positivity check, conservation sums) against FP64."""
+    """Accuracy of FP32 and FP64-fast against exact FP64 (bit-identical to the reference's
+    arithmetic) per configuration, in both reconstructions:
+
+    c1: 2048^2 four-quadrant (seeded rho, p ~ U[0.1,2], u, v ~ U[-1,1]), WENO5 + GQ + HLLE,
+        CFL 0.45; c2: oblique shock 4096x1024 on [0,4]x[0,1], seeded Mach ~ U[2,10] and
+        angle ~ U[30,75] deg, WENO5 + GQ + HLLC (blend 1e4/1.1e4), CFL 0.1, with the
+        oblique-shock inflow / outflow / reflecting-wall boundary.
+
+    The configurations name the characteristic reconstruction.  With the reference's
+    eigenvector matrices (its left eigenvectors carry 0.5/(rho c), so L R != I off
+    rho = 1) that scheme turns non-finite on both problems in exact FP64, i.e. in the
+    reference's own arithmetic; it is run up to the last finite step, and the
+    component-wise reconstruction for the configured step count (500 / 1000)."""
     import torch
     torch.cuda.set_device(0)
-    import weno_ext
     from weno_ext import problems
-    # The configurations name the characteristic-wise reconstruction.  With the
-    # reference's eigenvector matrices (L*R != I off rho = 1) that scheme produces
-    # NaN on these problems in every precision, the exact one included, so the
-    # accuracy runs use the component-wise reconstruction and the characteristic
-    # runs report the first step at which the reference algorithm turns non-finite.
-    recon = os.environ.get("WENO_ACC_RECON", "cons")
-    cons = recon == "cons"
     if args.config == "c1":
         nx, ny, nsteps = 2048, 2048, int(os.environ.get("WENO_C1_STEPS", "500"))
         q0 = problems.quadrant(nx, ny, seed=SEED + 1)
-        kw = dict(cons=cons, force_hlle=True, jp_cri=(0.2, 1.0), cfl=0.45)
-        runs = (("fp64_exact", 64, "exact"), ("fp64_fast", 64, "fast"), ("fp32", 32, "fast"))
+        kw = dict(force_hlle=True, jp_cri=(0.2, 1.0), cfl=0.45)
         dx, extra = 1.0 / 2048, {}
-        desc = f"four-quadrant Riemann {nx}x{ny}, {recon}-WENO5+GQ+HLLE, CFL 0.45, {nsteps} steps"
-        char_kw = dict(kw, cons=False)
+        desc = f"four-quadrant Riemann {nx}x{ny}, WENO5+GQ+HLLE, CFL 0.45"
     else:
         nx, ny, nsteps = 4096, 1024, int(os.environ.get("WENO_C2_STEPS", "1000"))
         rng = np.random.default_rng(SEED + 2)
         mach, theta = float(rng.uniform(2, 10)), math.radians(float(rng.uniform(30, 75)))
         q0, bound, post = problems.oblique_shock(nx, ny, 4.0, 1.0, mach, theta)
-        kw = dict(cons=cons, force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.1, bc="dmr", bound=bound, post=post)
-        runs = (("fp64_fast", 64, "fast"), ("fp32", 32, "fast"))
+        kw = dict(force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.1, bc="dmr", bound=bound, post=post)
         dx, extra = 1.0 / 1024, {"mach": mach, "theta_deg": math.degrees(theta), "bound": bound}
         desc = (f"oblique shock {nx}x{ny} on [0,4]x[0,1], M={mach:.3f}, angle={math.degrees(theta):.2f} deg, "
-                f"{recon}-WENO5+GQ+HLLC(blend 1e4/1.1e4), CFL 0.1, {nsteps} steps")
-        char_kw = dict(kw, cons=False)
-    # first non-finite step of the characteristic scheme (exact FP64 = the reference's arithmetic)
-    sc = weno_ext.Solver(nx, ny, dx, GAMMA, precision=64, mode="exact" if args.config == "c1" else "fast", **char_kw)
-    sc.set_state(q0)
-    blow = None
-    for k in range(0, nsteps, 5):
-        sc.run(5)
-        if sc.info()[2] & 1:
-            blow = sc.info()[1]
-            break
-    sc.close()
-    extra["characteristic_first_nonfinite_step"] = blow
-    res, states = {}, {}
-    for name, prec, mode in runs:
-        s = weno_ext.Solver(nx, ny, dx, GAMMA, precision=prec, mode=mode, **kw)
-        s.set_state(q0)
-        tot0 = s.totals()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(s.stream)
-        s.run(nsteps)
-        e1.record(s.stream)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1)
-        t, k, st = s.info()
-        tot1 = s.totals()
-        states[name] = s.state()
-        res[name] = {"steps": k, "t": t, "status": st, "ms_per_step": ms / nsteps,
-                     "cell_updates_per_s": nx * ny * k / (ms / 1e3), "totals_start": tot0, "totals_end": tot1,
-                     "nan": bool(np.isnan(states[name]).any())}
-        s.close()
-    ref = "fp64_exact" if "fp64_exact" in states else "fp64_fast"
-    errors = {name: _l1_linf(states[name], states[ref]) for name in states if name != ref}
+                "WENO5+GQ+HLLC(blend 1e4/1.1e4), CFL 0.1")
+    runs = (("fp64_exact", 64, "exact"), ("fp64_fast", 64, "fast"), ("fp32", 32, "fast"))
+    out = {}
+    blow = _first_nonfinite(nx, ny, dx, q0, dict(kw, cons=False), nsteps, "exact")
+    char_steps = nsteps if blow is None else blow - 1
+    marks = sorted({max(1, char_steps * f // 4) for f in (1, 2, 3, 4)})
+    res, errs = _lockstep(nx, ny, dx, q0, dict(kw, cons=False), runs, marks)
+    out["characteristic"] = {"steps": char_steps, "first_nonfinite_step_fp64_exact": blow, "runs": res,
+                             "errors_vs_fp64_exact": errs}
+    res, errs = _lockstep(nx, ny, dx, q0, dict(kw, cons=True), runs,
+                          sorted({nsteps * f // 4 for f in (1, 2, 3, 4)}))
+    out["component_wise"] = {"steps": nsteps, "runs": res, "errors_vs_fp64_exact": errs}
     line = {"metric": "accuracy and cell-updates/s", "config_name": args.config, "unit": UNIT, "n_gpus": 1,
-            "data": "synthetic", "config": dict({"workload": desc}, **extra), "runs": res,
-            "errors_vs_" + ref: errors}
+            "data": "synthetic", "config": dict({"workload": desc}, **extra), **out}
     print(json.dumps(line))
     return 0
 
 
-def run_c3(args):
+def batched_accuracy(nsolves, every=16):
+    """FP32 batched solves against FP64 (fast arithmetic, within 1e-10 of the reference's)
+    runs of the same solves: every `every`-th solve of the batched workload, to t_end."""
+    import weno_ext
+    from weno_ext import problems
+    rng = np.random.default_rng(SEED + 3)
+    shapes = problems.batch_shapes(nsolves, 64, 1024, SEED + 3)
+    t_ends = rng.uniform(0.1, 0.3, len(shapes))
+    pick = list(range(0, len(shapes), every))
+    states = {k: (problems.quadrant(*shapes[k], seed=SEED + k), 1.0 / max(shapes[k])) for k in pick}
+    kw = dict(mode="fast", cons=True, force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.5)
+    results = {}
+    for prec in (32, 64):
+        b = weno_ext.Batch(weno_ext.Batch.pool_cells([shapes[k] for k in pick], prec), len(pick), precision=prec,
+                           **kw)
+        slots = {k: b.add(states[k][0], states[k][1], t_end=float(t_ends[k])) for k in pick}
+        while b.poll()[0].any():
+            b.run(50)
+        results[prec] = {k: (b.info(sl), b.state(sl)) for k, sl in slots.items()}
+        b.close()
+    per, l1, linf = [], [], []
+    for k in pick:
+        i32, s32 = results[32][k]
+        i64, s64 = results[64][k]
+        if i32["status"] or i64["status"]:
+            per.append({"solve": k, "shape": shapes[k], "status": [i32["status"], i64["status"]]})
+            continue
+        e = _l1_linf(s32, s64)
+        l1.append(e["rho"]["rel_l1"])
+        linf.append(e["rho"]["rel_linf"])
+        per.append({"solve": k, "shape": shapes[k], "steps": [i32["steps"], i64["steps"]],
+                    "rho_rel_l1": e["rho"]["rel_l1"], "rho_rel_linf": e["rho"]["rel_linf"]})
+    return {"solves_compared": len(l1), "rho_rel_l1_max": max(l1) if l1 else None,
+            "rho_rel_l1_median": float(np.median(l1)) if l1 else None,
+            "rho_rel_linf_max": max(linf) if linf else None, "per_solve": per,
+            "reference": "FP64 batch, fast arithmetic (within 1e-10 relative L1 of exact FP64)"}
+
+
+def batched_leg(nsolves, tune=True):
     """Batched: independent four-quadrant solves of uneven size (edges log-uniform in
     [64, 1024], aspect <= 4), each with its own dt and t_end ~ U[0.1, 0.3], component
     WENO5 + HLLC (blend thresholds 1e4 / 1.1e4), FP32, CFL 0.5, all advanced together by
-    graph-replayed steps of the persistent tile kernels; the tile shape is autotuned."""
+    graph-replayed steps of the persistent tile kernels; the tile shape is autotuned.
+    Solves that reach t_end leave the batch between chunks of steps, so the tile list
+    holds only active solves.  Returns the result as a dict."""
     import torch
     torch.cuda.set_device(0)
     import weno_ext
     from weno_ext import autotune, problems
     rng = np.random.default_rng(SEED + 3)
-    shapes = problems.batch_shapes(args.solves, 64, 1024, SEED + 3)
+    shapes = problems.batch_shapes(nsolves, 64, 1024, SEED + 3)
     states = [(problems.quadrant(nx, ny, seed=SEED + k), 1.0 / max(nx, ny)) for k, (nx, ny) in enumerate(shapes)]
     t_ends = rng.uniform(0.1, 0.3, len(shapes))
     kw = dict(precision=32, mode="fast", cons=True, force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.5)
     sample = states[:: max(1, len(states) // 64)]
-    cfg, tune = autotune.best_tile_config(sample, **kw)
+    if tune:
+        cfg, tuning = autotune.best_tile_config(sample, **kw)
+    else:
+        cfg, tuning = 1, None
     cells = sum(nx * ny for nx, ny in shapes)
     b = weno_ext.Batch(weno_ext.Batch.pool_cells(shapes, 32), len(shapes), tile_config=cfg, **kw)
     slots = [b.add(q, dx, t_end=float(te)) for (q, dx), te in zip(states, t_ends)]
+    ntiles0 = b.stats()["tiles"]
     b.run(1)
     b.synchronize()
     done_before = b.poll()[2].copy()
     chunk = 20
+    final = {}
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    # steady state: every solve active (no solve finishes within the first chunk)
+    es0 = torch.cuda.Event(enable_timing=True)
+    es1 = torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
     e0.record(b.stream)
-    graph_steps = 0
+    es0.record(b.stream)
+    b.run(chunk)
+    es1.record(b.stream)
+    graph_steps = chunk
     while True:
+        act, tt, nn = b.poll()
+        for k, sl in enumerate(slots):
+            if k not in final and not act[sl]:
+                final[k] = (b.info(sl), int(nn[sl]))
+                b.remove(sl)
+        if len(final) == len(slots):
+            break
         b.run(chunk)
         graph_steps += chunk
-        act, tt, nn = b.poll()
-        if not act.any():
-            break
     e1.record(b.stream)
     e1.synchronize()
     wall = time.perf_counter() - t0
     ms = e0.elapsed_time(e1)
-    act, tt, nn = b.poll()
-    cu = int(sum(nx * ny * (int(n) - int(d)) for (nx, ny), n, d in zip(shapes, nn, done_before)))
+    steady_ms = es0.elapsed_time(es1)
+    steps = np.array([final[k][1] for k in range(len(slots))])
+    cu = int(sum(nx * ny * (int(n) - int(done_before[sl])) for (nx, ny), n, sl in zip(shapes, steps, slots)))
     st = b.stats()
     # Solves the reference scheme itself drives non-finite (component-wise WENO5 has no
     # positivity limiter) stop with a numeric status; the others must reach t_end.
-    failed = [k for k, sl in enumerate(slots) if b.info(sl)["status"] != 0]
+    failed = [k for k in range(len(slots)) if final[k][0]["status"] != 0]
     ok = [k for k in range(len(slots)) if k not in set(failed)]
-    line = {
-        "metric": "aggregate cell-updates/s, batched uneven four-quadrant solves (FP32)", "config_name": "c3",
-        "value": cu / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "dtype": "f32", "data": "synthetic",
+    tt = np.array([final[k][0]["t"] for k in range(len(slots))])
+    b.close()
+    return {
+        "metric": "aggregate cell-updates/s, batched uneven four-quadrant solves (FP32)",
+        "value": cu / (ms / 1e3), "unit": UNIT, "dtype": "f32",
         "config": {"workload": f"{len(shapes)} four-quadrant solves, edges log-uniform [64,1024], aspect<=4, "
                                "cons-WENO5+GQ+HLLC, FP32, CFL 0.5, t_end~U[0.1,0.3], per-solve dt",
-                   "cells": cells, "tiles": st["tiles"], "tile_config": cfg, "autotune_ms_per_step": tune},
+                   "cells": cells, "tiles": ntiles0, "tile_config": cfg, "autotune": tuning},
+        "steady_state": {"ms_per_step": steady_ms / chunk, "cell_updates_per_s": cells * chunk / (steady_ms / 1e3),
+                         "note": f"the first {chunk} graph-replayed steps, every solve active"},
         "steps_replayed": graph_steps, "cell_updates": cu, "gpu_ms": ms, "wall_s": wall,
         "launches_per_step": st["launches_per_step"],
-        "max_steps_of_a_solve": int(nn.max()), "min_steps_of_a_solve": int(nn.min()),
+        "max_steps_of_a_solve": int(steps.max()), "min_steps_of_a_solve": int(steps.min()),
         "solves_nonfinite": len(failed),
         "t_end_reached_by_the_others": bool(np.all(np.abs(tt[ok] - t_ends[ok]) < 1e-9)),
     }
+
+
+def run_c3(args):
+    line = batched_leg(args.solves)
+    line.update({"config_name": "c3", "n_gpus": 1, "data": "synthetic"})
+    if os.environ.get("WENO_C3_ACCURACY", "1") != "0":
+        line["fp32_vs_fp64"] = batched_accuracy(args.solves)
     print(json.dumps(line))
-    b.close()
     return 0
 
 
@@ -513,33 +605,77 @@ def run_dropin(args):
     return 0
 
 
-def run_c4(args):
+def serving_leg(nreq, rate, lo, hi, t_end, budget_gb, fp64_fraction=0.25, slabs=4, max_wait_s=None):
     """Serving: a seeded Poisson stream of requests (quadrant or oblique-shock initial
     data, FP32 or FP64 tag, seeded t_end) under an HBM budget with continuous batching."""
     import torch
     torch.cuda.set_device(0)
     from weno_ext import serving
-    lo, hi = int(os.environ.get("WENO_C4_LO", "128")), int(os.environ.get("WENO_C4_HI", "512"))
-    rate = float(os.environ.get("WENO_C4_RATE", "40"))
-    t_end = (float(os.environ.get("WENO_C4_TLO", "0.02")), float(os.environ.get("WENO_C4_THI", "0.06")))
-    budget = int(float(os.environ.get("WENO_C4_BUDGET_GB", "150")) * 1e9)
-    reqs = serving.poisson_stream(args.requests, rate=rate, lo=lo, hi=hi, seed=SEED + 4, fp64_fraction=0.25,
+    budget = int(budget_gb * 1e9)
+    reqs = serving.poisson_stream(nreq, rate=rate, lo=lo, hi=hi, seed=SEED + 4, fp64_fraction=fp64_fraction,
                                   t_end=t_end, shock_fraction=0.3)
-    srv = serving.Server(budget, fp64_share=0.5, max_solves=1024, steps_per_iter=8)
+    srv = serving.Server(budget, slabs=slabs, max_solves=1024, steps_per_iter=8, max_wait_s=max_wait_s)
     t0 = time.perf_counter()
     srv.serve(reqs, realtime=True)
     wall = time.perf_counter() - t0
+    conversions = srv.conversions
     srv.close()
     summ = serving.summarize(reqs, wall)
-    line = {"metric": "p50/p99 time-to-solution and aggregate cell-updates/s, serving stream", "config_name": "c4",
-            "value": summ["aggregate_cell_updates_per_s"], "unit": UNIT, "n_gpus": 1, "dtype": "f32+f64",
-            "data": "synthetic",
-            "config": {"workload": f"{args.requests} Poisson requests at {rate}/s, edges log-uniform [{lo},{hi}], "
-                                   f"t_end~U{t_end}, 25% FP64, 30% oblique shock, HBM budget {budget/1e9:.0f} GB",
-                       "steps_per_iteration": 8},
+    summ["slab_conversions"] = conversions
+    # work of each request (cells x steps) against its time to solution: the tail is
+    # the largest requests, whose work spans more than three decades over [lo, hi]
+    work = np.array([r.cells * r.steps for r in reqs if r.status == 0])
+    tts = np.array([r.finished - r.arrival for r in reqs if r.status == 0])
+    if len(work) > 2:
+        summ["work_p50_over_p99"] = float(np.percentile(work, 50) / max(np.percentile(work, 99), 1))
+        summ["corr_log_work_log_tts"] = float(np.corrcoef(np.log(work + 1), np.log(tts + 1e-9))[0, 1])
+    return {"metric": "p50/p99 time-to-solution and aggregate cell-updates/s, serving stream",
+            "value": summ["aggregate_cell_updates_per_s"], "unit": UNIT, "dtype": "f32+f64",
+            "config": {"workload": f"{nreq} Poisson requests at {rate}/s, edges log-uniform [{lo},{hi}], "
+                                   f"t_end~U{tuple(t_end)}, {int(100 * fp64_fraction)}% FP64, 30% oblique shock, "
+                                   f"HBM budget {budget / 1e9:.0f} GB in {slabs} slabs",
+                       "steps_per_iteration": 8, "max_wait_s": max_wait_s},
             "serving": summ}
+
+
+def run_c4(args):
+    lo, hi = int(os.environ.get("WENO_C4_LO", "128")), int(os.environ.get("WENO_C4_HI", "2048"))
+    rate = float(os.environ.get("WENO_C4_RATE", "10"))
+    t_end = (float(os.environ.get("WENO_C4_TLO", "0.001")), float(os.environ.get("WENO_C4_THI", "0.003")))
+    budget = float(os.environ.get("WENO_C4_BUDGET_GB", "150"))
+    wait = os.environ.get("WENO_C4_MAX_WAIT")
+    line = serving_leg(args.requests, rate, lo, hi, t_end, budget, max_wait_s=float(wait) if wait else None)
+    line.update({"config_name": "c4", "n_gpus": 1, "data": "synthetic"})
     print(json.dumps(line))
     return 0
+
+
+def dropin_host_leg(nx, ny, calls=3):
+    """The reference's calling convention: l_local_py on numpy arrays of the drivers'
+    (nx+6, ny+6, 8) layout, host copies in and out inside every call, both arithmetic
+    modes.  Unit: cell-residuals/s (interior cells whose L(U) one call evaluates)."""
+    import weno_ext
+    q = quadrant_state(nx, ny)
+    dx = 1.0 / nx
+    out = {}
+    prev = weno_ext.get_mode()
+    try:
+        for mode in ("fast", "exact"):
+            weno_ext.set_mode(mode)
+            weno_ext.l_local_py(q, dx, GAMMA, True, (0.2, 1.0), False)
+            t0 = time.perf_counter()
+            for _ in range(calls):
+                weno_ext.l_local_py(q, dx, GAMMA, True, (0.2, 1.0), False)
+            ms = (time.perf_counter() - t0) * 1e3 / calls
+            out[mode] = {"ms_per_call": ms, "value": nx * ny / (ms / 1e3)}
+    finally:
+        weno_ext.set_mode(prev)
+    M, N = nx + 6, ny + 6
+    return {"value": out["fast"]["value"], "unit": "cell-residuals/s", "modes": out,
+            "h2d_bytes_per_call": M * N * 8 * 8, "d2h_bytes_per_call": nx * ny * 4 * 8,
+            "path": "weno_ext.l_local_py(numpy (nx+6, ny+6, 8) f64, dx, 1.4, True, (0.2, 1.0), False) -> numpy "
+                    "(nx, ny, 4); char-WENO5+GQ+HLLE, one residual per call",
+            "calls": calls}
 
 
 def time_solver(Solver, q0, nx, ny, steps, warmup, **kw):
@@ -580,6 +716,9 @@ def main():
                          "dropin: the weno_ext functions themselves (l_local_py & co.)")
     ap.add_argument("--solves", type=int, default=512)
     ap.add_argument("--requests", type=int, default=300)
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched (512 solves) leg of the default line")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream leg of the default line")
+    ap.add_argument("--no-dropin", action="store_true", help="skip the numpy l_local_py leg of the default line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -662,6 +801,14 @@ def main():
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"}
+    # The whole step against the minimal fused traffic of one cell-update: 32 values
+    # (stage 1 reads 4, writes 4; stages 2 and 3 read 8, write 4), 256 B in FP64.
+    step_bytes = 32 * (4 if args.precision == "f32" else 8) * nx * ny
+    step_gbs = step_bytes / (ms / args.steps / 1e3) / 1e9
+    roofline["step"] = {"algorithmic_bytes_per_step": step_bytes, "achieved": step_gbs, "unit": "GB/s",
+                        "frac": step_gbs / hbm_peak,
+                        "note": "32 values per cell-update (minimal fused SSP-RK3 traffic) x cells / ms_per_step"}
+    roofline["step_frac_8d"] = step_gbs / hbm_peak
     pipe = prof.get("fp64_pipe_pct_of_peak") if args.precision == "f64" else None
     if pipe:
         # The HBM fraction is the contract's denominator; the pipe that binds these kernels is FP64.
@@ -752,11 +899,26 @@ def main():
         "variants": variants,
         "status": {"sim_time": t_sim, "steps_done": nsteps_done, "numeric_status": status},
     }
+    line["parity"] = {
+        "exact_vs_oracle": "bit-identical after 2 steps of this workload at 4096^2 "
+                           "(tests/test_gpu_headline.py)",
+        "fast_vs_exact": "relative L1 <= 1e-10 per conserved variable after 25 steps of this workload "
+                         "(tests/test_gpu_headline.py; measured 2.4e-16)"}
+    s.close()
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(nx, int(os.environ.get("WENO_CPU_STRIP", "32")), os.cpu_count() or 1)
+    if rank == 0 and world == 1 and args.precision == "f64":
+        # The other figures BASELINE's metric names, on the same box in the same run.
+        torch.cuda.empty_cache()
+        if not args.no_dropin:
+            line["e2e_dropin"] = dropin_host_leg(nx, ny)
+        if not args.no_batched:
+            line["batched"] = batched_leg(args.solves)
+        if not args.no_serving:
+            line["serving"] = serving_leg(int(os.environ.get("WENO_SERVE_REQUESTS", "200")), 20.0, 128, 2048,
+                                          (0.001, 0.003), 150.0)
     if rank == 0:
         print(json.dumps(line))
-    s.close()
     replicas.finish()
     return 0
 
