@@ -260,3 +260,53 @@ def test_nan_density_stops_the_solver(wx, orc, sign, smode):
     assert st & 1
     assert np.isnan(s.state()[3:-3, 3:-3, :4]).all()
     s.close()
+
+
+@pytest.mark.parametrize("ydir", [0, 1], ids=["x", "y"])
+def test_fast_riemann_on_mirror_faces(wx, orc, ydir):
+    """At a reflecting wall the two face states are mirror images (normal momentum
+    negated).  Where the energy has gone negative the Roe sound speed is zero, and the
+    reference flux switches from F_L to F_R with the sign of the Roe-averaged normal
+    velocity, which its arithmetic makes exactly +0.0.  FAST mode must land on the same
+    side: every solver agrees with the oracle to the one-call tolerance."""
+    rng = np.random.default_rng(21 + ydir)
+    m, n = 16, 24
+    ql = np.ascontiguousarray(noisy(rng, m, n)[:, :, :4])
+    ql[rng.random((m, n)) < 0.4, 3] *= -1.0  # negative energy: zero Roe sound speed
+    qr = ql.copy()
+    qr[:, :, 2 if ydir else 1] *= -1.0
+    flux = orc.flux_y_py if ydir else orc.flux_x_py
+    fl, fr = flux(ql, G), flux(qr, G)
+    solvers = ((wx.hlle_y_rs_py, orc.hlle_y_rs_py), (wx.hllc_y_rs_py, orc.hllc_y_rs_py)) if ydir else \
+              ((wx.hlle_x_rs_py, orc.hlle_x_rs_py), (wx.hllc_x_rs_py, orc.hllc_x_rs_py))
+    wx.set_mode("fast")
+    try:
+        for fw, fo in solvers:
+            check(fw(ql, fl, qr, fr, G), fo(ql, fl, qr, fr, G), "fast", fw.__name__)
+        bw = wx.hllc_hlle_y_rs_py if ydir else wx.hllc_hlle_x_rs_py
+        bo = orc.hllc_hlle_y_rs_py if ydir else orc.hllc_hlle_x_rs_py
+        check(bw(ql, fl, qr, fr, G, 0.05, 0.4, False), bo(ql, fl, qr, fr, G, 0.05, 0.4, False), "fast", "blend")
+    finally:
+        wx.set_mode("exact")
+
+
+@pytest.mark.parametrize("cons", [True], ids=["cons"])
+def test_fast_reconstruction_mirror_exact(wx, cons):
+    """Mirror-image stencils (the reflecting wall): FAST's left and right face states of
+    a face whose six cells are mirror images are themselves exact mirrors (normal
+    momentum negated), as the reference's arithmetic makes them."""
+    rng = np.random.default_rng(33)
+    m, n = 12, 10
+    half = noisy(rng, m, n // 2)
+    q = np.concatenate([half[:, ::-1], half], axis=1)  # columns j and n-1-j mirror each other
+    q[:, : n // 2, 2] *= -1.0  # the normal (y) momentum flips across the wall
+    q = np.ascontiguousarray(q)
+    wx.set_mode("fast")
+    try:
+        ql, fl, qr, fr = wx.weno_y_py(q, G, cons=cons)
+    finally:
+        wx.set_mode("exact")
+    # the wall face is face column n//2 - 3 of the (m-6, n-5) face arrays
+    c = n // 2 - 3
+    sign = np.array([1.0, 1.0, -1.0, 1.0])
+    assert np.array_equal(ql[:, c, :], qr[:, c, :] * sign)

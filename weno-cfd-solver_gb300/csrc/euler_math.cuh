@@ -116,6 +116,21 @@ __device__ __forceinline__ T frsqrt(T x) {
   else return T(1.0) / sqrt(x);
 }
 
+// a*b + c*d with both products rounded on their own (never contracted into an
+// FMA).  For mirror-image arguments (c*d = -(a*b) exactly) the sum is +0.0, as
+// the reference's separately rounded products give; a fused form would leave
+// the first product's rounding error, a tiny value of either sign.  Used where
+// a sign decides a branch: the Roe-averaged normal velocity and the HLLC star
+// speed at a reflecting wall, where the reference flux jumps from F_L to F_R as
+// that sign changes (when the Roe sound speed is zero, e.g. a state whose
+// energy has gone negative).
+template <class T>
+__device__ __forceinline__ T sum_prod_rn(T a, T b, T c, T d) {
+  if constexpr (is_native_f64<T>) return __dadd_rn(__dmul_rn(a, b), __dmul_rn(c, d));
+  else if constexpr (is_f32<T>) return __fadd_rn(__fmul_rn(a, b), __fmul_rn(c, d));
+  else return a * b + c * d;
+}
+
 // ---------------------------------------------------------------------------
 // Conserved state helpers (utils.rs:9-35, utils.rs:74-109)
 // ---------------------------------------------------------------------------
@@ -371,16 +386,21 @@ __device__ __forceinline__ void weno5_lr_fast(T u0, T u1, T u2, T u3, T u4, T u5
   // candidate polynomials (x6): the right stencil's p1, p2 are the left's p0, p1
   const T pl0 = -u4 + T(5.0) * u3 + T(2.0) * u2, pl1 = -u1 + T(5.0) * u2 + T(2.0) * u3;
   const T pl2 = T(2.0) * u0 - T(7.0) * u1 + T(11.0) * u2, pr0 = T(2.0) * u5 - T(7.0) * u4 + T(11.0) * u3;
+  // The right reconstruction takes its stencils in the mirror order of the left
+  // one (1-3, 2-4, 3-5 against 2-4, 1-3, 0-2), so that for mirror-image inputs
+  // (u_k -> u_{5-k}, as across a reflecting wall) it performs the left one's
+  // operations on bit-identical values and the two face states are exact
+  // mirrors, as in the reference's arithmetic.
   if constexpr (is_native_f64<T>) {
-    // linear weights scaled by 10 -- (3, 6, 1) and (1, 6, 3) -- and the 1/6 of
-    // the candidate polynomials applied once to the shared divide
+    // linear weights scaled by 10 -- (3, 6, 1) -- and the 1/6 of the candidate
+    // polynomials applied once to the shared divide
     double nl, dl, nr, dr;
     weno_nd(el0, el1, el2, 3.0, 6.0, 1.0, pl0, pl1, pl2, 1.0, nl, dl);
-    weno_nd(er0, er1, er2, 1.0, 6.0, 3.0, pr0, pl0, pl1, 1.0, nr, dr);
+    weno_nd(er2, er1, er0, 3.0, 6.0, 1.0, pl1, pl0, pr0, 1.0, nr, dr);
     div_pair(nl, dl, nr, dr, left, right, 6.0);
   } else {
     left = weno_combine<T, true>(el0, el1, el2, T(0.3), T(0.6), T(0.1), pl0, pl1, pl2, T(6.0));
-    right = weno_combine<T, true>(er0, er1, er2, T(0.1), T(0.6), T(0.3), pr0, pl0, pl1, T(6.0));
+    right = weno_combine<T, true>(er2, er1, er0, T(0.3), T(0.6), T(0.1), pl1, pl0, pr0, T(6.0));
   }
 }
 
@@ -777,8 +797,8 @@ __device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], con
   } else {
     // sqrt(rho) = rho r and sqrt(rho)*h = (E+p) r with r = 1/sqrt(rho) per side.
     const T id = qrcp<T, FAST>(r.ql0 * rsl + r.qr0 * rsr);
-    u_t = (ql[1] * rsl + qr[1] * rsr) * id;
-    v_t = (ql[2] * rsl + qr[2] * rsr) * id;
+    u_t = sum_prod_rn<T>(ql[1], rsl, qr[1], rsr) * id;
+    v_t = sum_prod_rn<T>(ql[2], rsl, qr[2], rsr) * id;
     h_t = ((ql[3] + r.p_l) * rsl + (qr[3] + r.p_r) * rsr) * id;
   }
   const T tmp = h_t - T(0.5) * (u_t * u_t + v_t * v_t);
@@ -838,8 +858,14 @@ __device__ __forceinline__ void hllc_flux(const RiemannPre<T, FAST, Y>& r, const
     return;
   }
   const T denom = guard_denom<T, FAST>(r.ql0 * (r.s_l - r.un_l) - r.qr0 * (r.s_r - r.un_r));
-  const T s_star = qdiv<T, FAST>(
-      r.p_r - r.p_l + r.ql0 * r.un_l * (r.s_l - r.un_l) - r.qr0 * r.un_r * (r.s_r - r.un_r), denom);
+  // FAST: the two momentum terms rounded on their own, so mirror-image states give
+  // S* = +0.0 exactly, as the reference's arithmetic does
+  const T s_star = FAST ? qdiv<T, FAST>((r.p_r - r.p_l) + sum_prod_rn<T>(r.ql0 * r.un_l, r.s_l - r.un_l,
+                                                                           -(r.qr0 * r.un_r), r.s_r - r.un_r),
+                                        denom)
+                        : qdiv<T, FAST>(r.p_r - r.p_l + r.ql0 * r.un_l * (r.s_l - r.un_l) -
+                                            r.qr0 * r.un_r * (r.s_r - r.un_r),
+                                        denom);
   if (r.s_l < T(0.0) && s_star >= T(0.0)) {
     // left star state
     const T m_l = r.ql0 * (r.s_l - r.un_l);
