@@ -177,15 +177,25 @@ int weno_solver_launches_per_step(weno_solver* s);
  * only its interior cells stored in a packed pool of `pool_cells` cells per RK
  * buffer.  One step of ALL active solves is five launches: the per-solve dt,
  * three persistent stage kernels that walk a packed list of TX x TY tiles
- * (tile shape `tile_config`, 0..weno_batch_tile_config_count()-1) and fuse
- * the whole residual with the stage combination in shared memory, and the
- * clock update; the boundary fill is applied while tiles load.  Solves can be
+ * (tile shape `tile_config`, 0..3) and fuse the whole residual with the stage
+ * combination in shared memory, and the clock update; the boundary fill is
+ * applied while tiles load.  tile_config 4 is the staged variant: each stage
+ * is three launches (pass 1 of every face, pass 2 with the Riemann solvers,
+ * residual with the combination) over 16 x 32 tiles, with the face states and
+ * fluxes in a device workspace the batch owns (weno_batch_bytes_per_cell), so
+ * no face is computed twice -- faster where the arithmetic pipe binds and
+ * HBM has room (FP64).  Solves can be
  * added and removed between runs (continuous batching).  Results of a solve
  * do not depend on the other solves in the batch.
  * ---------------------------------------------------------------------- */
 typedef struct weno_batch weno_batch;
 
 int weno_batch_tile_config_count(void);
+/* Device bytes one pool cell costs in a batch of this precision, flux choice and
+ * tile configuration: the three RK pools, plus (staged configuration) the
+ * share of the face workspace reserved per cell.  pool_cells x this is about
+ * what weno_batch_create allocates. */
+double weno_batch_bytes_per_cell(int precision, int force_hlle, int tile_config);
 int weno_batch_create(weno_batch** out, int64_t pool_cells, int max_solves, int precision, int mode, int cons,
                       int force_hlle, double gamma, double jp_lo, double jp_hi, double cfl, double weno_eps,
                       int tile_config, void* stream);

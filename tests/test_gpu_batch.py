@@ -20,7 +20,7 @@ def synced(orc, q):
 
 
 @pytest.mark.parametrize("cons,hlle", [(False, True), (True, False), (False, False), (True, True)])
-@pytest.mark.parametrize("cfg", [0, 1, 2, 3])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
 def test_exact_batch_matches_oracle(wx, orc, cons, hlle, cfg):
     rng = np.random.default_rng(100 + cfg)
     shapes = [(21, 13), (9, 40), (33, 33)]

@@ -97,6 +97,11 @@ struct weno_batch {
   int add_tile_cap = 0;
   // free list: offset -> length (elements)
   std::map<long long, long long> free_list;
+  // staged configuration: the face workspace pool (elements) and its free list
+  void* ws_base = nullptr;
+  long long ws_capacity = 0;
+  std::map<long long, long long> ws_free;
+  std::vector<long long> ws_off, ws_len;  // per slot
   cudaGraphExec_t graph = nullptr;
   int graph_ntiles = -1;
   // test hook (weno_batch_debug_skip_copy): tile whose staging copy is not issued,
@@ -114,6 +119,15 @@ cudaError_t enqueue_batch_step(weno_batch* b) {
   const int grid = b->fixed_grid > 0 ? b->fixed_grid : std::min(b->ntiles, b->sm_count * b->occ);
   cudaError_t e;
   if ((e = BL::clock(b->d_ctl, b->max_solves, 0, b->stream))) return e;
+  if (b->cfg == kStagedConfig) {
+    for (int s = 1; s <= 3; ++s) {
+      void* qo = b->pool[s == 1 ? 1 : (s == 2 ? 2 : 0)];
+      if ((e = BL::staged(b->chr, b->blend, b->d_solves, b->d_ctl, b->d_tiles, b->ntiles, grid, b->pool[s - 1],
+                          b->pool[0], qo, b->ws_base, s, b->gamma, b->jp_lo, b->jp_hi, b->weps, b->stream)))
+        return e;
+    }
+    return BL::clock(b->d_ctl, b->max_solves, 1, b->stream);
+  }
   for (int s = 1; s <= 3; ++s) {
     // stage s reads pool s-1 (q, q1, q2) through the tensor maps
     void* qo = b->pool[s == 1 ? 1 : (s == 2 ? 2 : 0)];
@@ -173,34 +187,65 @@ int rebuild_tiles(weno_batch* b) {
   return WENO_OK;
 }
 
-long long pool_alloc(weno_batch* b, long long len) {
+long long fl_alloc(std::map<long long, long long>& fl, long long len) {
   len = align64(len);
-  for (auto it = b->free_list.begin(); it != b->free_list.end(); ++it) {
+  for (auto it = fl.begin(); it != fl.end(); ++it) {
     if (it->second >= len) {
       const long long off = it->first, rest = it->second - len;
-      b->free_list.erase(it);
-      if (rest > 0) b->free_list[off + len] = rest;
+      fl.erase(it);
+      if (rest > 0) fl[off + len] = rest;
       return off;
     }
   }
   return -1;
 }
 
-void pool_free(weno_batch* b, long long off, long long len) {
+void fl_free(std::map<long long, long long>& fl, long long off, long long len) {
   len = align64(len);
-  auto it = b->free_list.emplace(off, len).first;
+  auto it = fl.emplace(off, len).first;
   auto next = std::next(it);
-  if (next != b->free_list.end() && it->first + it->second == next->first) {
+  if (next != fl.end() && it->first + it->second == next->first) {
     it->second += next->second;
-    b->free_list.erase(next);
+    fl.erase(next);
   }
-  if (it != b->free_list.begin()) {
+  if (it != fl.begin()) {
     auto prev = std::prev(it);
     if (prev->first + prev->second == it->first) {
       prev->second += it->second;
-      b->free_list.erase(it);
+      fl.erase(it);
     }
   }
+}
+
+long long pool_alloc(weno_batch* b, long long len) { return fl_alloc(b->free_list, len); }
+void pool_free(weno_batch* b, long long off, long long len) { fl_free(b->free_list, off, len); }
+
+// Face workspace of one solve in the staged configuration (element counts; see
+// k_staged_pass1): fills the layout fields of `d` with offsets relative to the
+// solve's block and returns the block's length.
+long long staged_layout(SolveDesc& d, int lq, int nf) {
+  auto up = [lq](long long x) { return (x + lq - 1) / lq * lq; };
+  const long long nx = d.nx, ny = d.ny;
+  d.l_p1x = (int)up(ny + 4);
+  d.l_p1y = (int)up(ny + 1);
+  d.s_p1x = align64((nx + 1) * d.l_p1x);
+  d.s_p1y = align64((nx + 4) * d.l_p1y);
+  d.s_fx = align64((nx + 1) * d.ld);
+  d.s_fy = align64(nx * d.l_p1y);
+  d.w_p1x = 0;
+  d.w_p1y = 8 * d.s_p1x;
+  d.w_fx = d.w_p1y + 8 * d.s_p1y;
+  d.w_fy = d.w_fx + nf * d.s_fx;
+  return d.w_fy + nf * d.s_fy;
+}
+
+// Workspace elements reserved per pool cell in the staged configuration: the
+// face arrays of a solve take about 16 + 2 NF values per cell, more for small
+// grids (halo rows and columns, 64-element plane alignment).
+constexpr double kStagedWsPerCellMargin = 1.25;
+inline long long staged_ws_capacity(long long pool_cells, int max_solves, int nf) {
+  return align64((long long)(kStagedWsPerCellMargin * (16 + 2 * nf) * (double)pool_cells) +
+                 (long long)max_solves * (16 + 2 * nf) * 128);
 }
 
 // Installs a host-encoded tensor map (passed by value) at `dst` in global
@@ -260,6 +305,7 @@ void batch_free(weno_batch* b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   cudaFree(b->pool_base);
+  cudaFree(b->ws_base);
   cudaFree(b->d_tmaps);
   cudaFree(b->d_solves);
   cudaFree(b->d_ctl);
@@ -314,16 +360,20 @@ int weno_batch_create(weno_batch** out, int64_t pool_cells, int max_solves, int 
   int dev = 0;
   if ((e = cudaGetDevice(&dev))) return bail(e, "cudaGetDevice");
   if ((e = cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev))) return bail(e, "attr");
-  const size_t smem = precision == 32 ? BatchLaunch<float, true>::smem_bytes(b->cfg, b->blend)
-                      : (b->mode == WENO_FAST ? BatchLaunch<double, true>::smem_bytes(b->cfg, b->blend)
-                                              : BatchLaunch<double, false>::smem_bytes(b->cfg, b->blend));
-  if (!smem) {
-    batch_free(b);
-    return bfail(WENO_ERR_ARG, "batch_create: tile configuration %d does not fit in shared memory", tile_config);
+  if (b->cfg == kStagedConfig) {
+    b->occ = 8;  // grid of the staged kernels: up to 8 CTAs of 256 threads per SM walk the tile list
+  } else {
+    const size_t smem = precision == 32 ? BatchLaunch<float, true>::smem_bytes(b->cfg, b->blend)
+                        : (b->mode == WENO_FAST ? BatchLaunch<double, true>::smem_bytes(b->cfg, b->blend)
+                                                : BatchLaunch<double, false>::smem_bytes(b->cfg, b->blend));
+    if (!smem) {
+      batch_free(b);
+      return bfail(WENO_ERR_ARG, "batch_create: tile configuration %d does not fit in shared memory", tile_config);
+    }
+    b->occ = std::max(1, precision == 32 ? BatchLaunch<float, true>::ctas_per_sm(b->cfg, b->chr, b->blend)
+                         : (b->mode == WENO_FAST ? BatchLaunch<double, true>::ctas_per_sm(b->cfg, b->chr, b->blend)
+                                                 : BatchLaunch<double, false>::ctas_per_sm(b->cfg, b->chr, b->blend)));
   }
-  b->occ = std::max(1, precision == 32 ? BatchLaunch<float, true>::ctas_per_sm(b->cfg, b->chr, b->blend)
-                       : (b->mode == WENO_FAST ? BatchLaunch<double, true>::ctas_per_sm(b->cfg, b->chr, b->blend)
-                                               : BatchLaunch<double, false>::ctas_per_sm(b->cfg, b->chr, b->blend)));
   if (!encode_tiled()) {
     batch_free(b);
     return bfail(WENO_ERR_CUDA, "batch_create: cuTensorMapEncodeTiled is not available from the driver");
@@ -338,6 +388,16 @@ int weno_batch_create(weno_batch** out, int64_t pool_cells, int max_solves, int 
       return bail(e, "cudaMemsetAsync(pool)");
   }
   for (int k = 0; k < 3; ++k) b->pool[k] = static_cast<char*>(b->pool_base) + (size_t)k * b->capacity * b->es;
+  b->ws_off.assign(max_solves, -1);
+  b->ws_len.assign(max_solves, 0);
+  if (b->cfg == kStagedConfig) {
+    b->ws_capacity = staged_ws_capacity(pool_cells, max_solves, b->blend ? 9 : 4);
+    if ((e = cudaMalloc(&b->ws_base, (size_t)b->ws_capacity * b->es))) return bail(e, "cudaMalloc(workspace)");
+    const char* v = std::getenv("WENO_DEBUG_NAN_FILL");
+    if (v && v[0] && v[0] != '0' && (e = cudaMemsetAsync(b->ws_base, 0xFF, (size_t)b->ws_capacity * b->es, b->stream)))
+      return bail(e, "cudaMemsetAsync(workspace)");
+    b->ws_free[0] = b->ws_capacity;
+  }
   if ((e = cudaMalloc(&b->d_tmaps, sizeof(CUtensorMap) * max_solves))) return bail(e, "cudaMalloc(tensor maps)");
   b->h_tmaps.assign(max_solves, CUtensorMap{});
   if ((e = cudaMalloc(&b->d_solves, sizeof(SolveDesc) * max_solves))) return bail(e, "cudaMalloc(solves)");
@@ -414,6 +474,20 @@ int weno_batch_add(weno_batch* b, int64_t nx, int64_t ny, double dx, int bc_kind
   d.dx = dx;
   if (post8)
     for (int k = 0; k < 8; ++k) d.post[k] = post8[k];
+  if (b->cfg == kStagedConfig) {
+    const long long len = staged_layout(d, lq, b->blend ? 9 : 4);
+    const long long woff = fl_alloc(b->ws_free, len);
+    if (woff < 0) {
+      pool_free(b, off, 4 * ps);
+      return bfail(WENO_ERR_WORKSPACE, "batch_add: face workspace full (%lld elements requested)", len);
+    }
+    d.w_p1x += woff;
+    d.w_p1y += woff;
+    d.w_fx += woff;
+    d.w_fy += woff;
+    b->ws_off[slot] = woff;
+    b->ws_len[slot] = len;
+  }
   b->h_solves[slot] = d;
   b->used[slot] = true;
   WB_CK(cudaMemcpyAsync(b->d_solves + slot, &b->h_solves[slot], sizeof(SolveDesc), cudaMemcpyHostToDevice, b->stream));
@@ -468,6 +542,10 @@ int weno_batch_remove(weno_batch* b, int slot) {
   if (!b || slot < 0 || slot >= b->max_solves || !b->used[slot]) return bfail(WENO_ERR_ARG, "batch_remove: bad slot");
   WB_CK(cudaStreamSynchronize(b->stream));
   pool_free(b, b->h_solves[slot].off, 4 * b->h_solves[slot].ps);
+  if (b->ws_off[slot] >= 0) {
+    fl_free(b->ws_free, b->ws_off[slot], b->ws_len[slot]);
+    b->ws_off[slot] = -1;
+  }
   b->used[slot] = false;
   SolveCtl zero{};
   WB_CK(cudaMemcpy(b->d_ctl + slot, &zero, sizeof(SolveCtl), cudaMemcpyHostToDevice));
@@ -544,6 +622,13 @@ int weno_batch_poll(weno_batch* b, int* active, double* t, int64_t* steps) {
     if (steps) steps[s] = b->h_ctl[s].steps;
   }
   return WENO_OK;
+}
+
+double weno_batch_bytes_per_cell(int precision, int force_hlle, int tile_config) {
+  const double es = precision == 32 ? 4.0 : 8.0;
+  double values = 12.0;  // three RK pools of four conserved planes
+  if (tile_config == kStagedConfig) values += kStagedWsPerCellMargin * (16 + 2 * (force_hlle ? 4 : 9));
+  return values * es;
 }
 
 int weno_batch_debug_skip_copy(weno_batch* b, int tile, int64_t wait_ns, int grid) {

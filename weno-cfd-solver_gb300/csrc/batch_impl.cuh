@@ -52,6 +52,7 @@ int occupancy() {
 }  // namespace bdetail
 }  // inline namespace WENO_TU_NS
 
+// Fused configurations only (0-3); the staged configuration has its own launcher.
 #define WENO_TILE_SWITCH(cfg, MACRO) \
   switch (cfg) {                     \
     case 0: MACRO(8, 32); break;     \
@@ -119,6 +120,39 @@ cudaError_t BatchLaunch<T, FAST>::stage(int cfg, bool chr, bool blend, const Sol
   WENO_TILE_SWITCH(cfg, WENO_ST)
 #undef WENO_ST
   return e;
+}
+
+template <class T, bool FAST>
+cudaError_t BatchLaunch<T, FAST>::staged(bool chr, bool blend, const SolveDesc* solves, SolveCtl* ctl,
+                                         const void* tiles, int ntiles, int grid, const void* qs, const void* qn,
+                                         void* qo, void* ws, int stage, double gamma, double jp_lo, double jp_hi,
+                                         double weps, cudaStream_t st) {
+  if (ntiles <= 0 || grid <= 0) return cudaSuccess;
+  constexpr int TX = kTileTX[kStagedConfig], TY = kTileTY[kStagedConfig], NT = bdetail::kNT;
+  const int4* tl = static_cast<const int4*>(tiles);
+  T* W = static_cast<T*>(ws);
+  const T* Qs = static_cast<const T*>(qs);
+  if (chr)
+    k_staged_pass1<T, FAST, true, TX, TY, NT><<<grid, NT, 0, st>>>(solves, ctl, tl, ntiles, Qs, W, (T)gamma, (T)weps);
+  else
+    k_staged_pass1<T, FAST, false, TX, TY, NT><<<grid, NT, 0, st>>>(solves, ctl, tl, ntiles, Qs, W, (T)gamma,
+                                                                     (T)weps);
+  cudaError_t e = cudaGetLastError();
+  if (e) return e;
+  if (blend)
+    k_staged_pass2<T, FAST, true, TX, TY, NT><<<grid, NT, 0, st>>>(solves, ctl, tl, ntiles, W, (T)gamma, (T)weps);
+  else
+    k_staged_pass2<T, FAST, false, TX, TY, NT><<<grid, NT, 0, st>>>(solves, ctl, tl, ntiles, W, (T)gamma, (T)weps);
+  if ((e = cudaGetLastError())) return e;
+  const T* Qn = static_cast<const T*>(qn);
+  T* Qo = static_cast<T*>(qo);
+  if (blend)
+    k_staged_residual<T, FAST, true, TX, TY, NT><<<grid, NT, 0, st>>>(solves, ctl, tl, ntiles, W, Qs, Qn, Qo, stage,
+                                                                       (T)gamma, (T)jp_lo, (T)jp_hi);
+  else
+    k_staged_residual<T, FAST, false, TX, TY, NT><<<grid, NT, 0, st>>>(solves, ctl, tl, ntiles, W, Qs, Qn, Qo,
+                                                                        stage, (T)gamma, (T)jp_lo, (T)jp_hi);
+  return cudaGetLastError();
 }
 
 template <class T, bool FAST>

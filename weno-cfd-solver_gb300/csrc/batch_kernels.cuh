@@ -35,6 +35,11 @@ struct SolveDesc {
   int bound;      // DMR: last row of the inflow segment on the lower boundary
   double dx;      // cell size (dx = dy)
   double post[8]; // DMR inflow state: conserved channels 0..3, primitive channels 4..7
+  // Staged tile configuration only: this solve's face workspace, element offsets
+  // in the workspace pool (see k_staged_pass1).
+  long long w_p1x, w_p1y, w_fx, w_fy;  // plane 0 of each array
+  long long s_p1x, s_p1y, s_fx, s_fy;  // plane strides
+  int l_p1x, l_p1y;                    // row pitches of P1x and of P1y / Fy (Fx uses ld)
 };
 
 struct SolveCtl {
@@ -487,6 +492,265 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
     // accesses before it
     tma::fence_proxy_async_smem();
     __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Staged variant: the arithmetic of k_stage_tiles in three launches per stage,
+// with the pass-1 face states and the face fluxes of every solve in a global
+// workspace instead of shared memory, so each face is reconstructed once (the
+// fused kernel recomputes the halo faces of every tile, 1.2-1.5x the pass-1
+// work at 16 x 32).  In FP64 the kernels are bound by the FP64 pipe and HBM is
+// nearly idle, so moving the faces through HBM and L2 costs less than that
+// recompute.  Per solve (interior nx x ny):
+//   P1x  8 planes (q_l, q_r) of (nx+1) x (ny+4): face row fi, column c <-> J = c-2
+//   P1y  8 planes of (nx+4) x (ny+1): row r <-> I = r-2, face column fj
+//   Fx   NF planes of (nx+1) x ny (pitch ld), Fy NF planes of nx x (ny+1)
+//        (NF = 4: HLLE; 9: HLLC, HLLE and the mean pressure of the sensor blend)
+// The work of a launch is the packed cell-tile list: a tile (i0, j0) owns its
+// own faces, and the tiles on a solve's edges also own the faces beyond it.
+// ---------------------------------------------------------------------------
+
+// The four conserved values of padded cell (I, J) of a solve: from the pool
+// (interior cells only) or, for a ghost cell, from the cell (or inflow state)
+// the boundary fill would copy there.
+template <class T>
+__device__ __forceinline__ void staged_cell(const SolveDesc& d, const T* q, int I, int J, T v[4]) {
+  int i = I - 3, j = J - 3;
+  bool flip = false;
+  if (i < 0 || i >= d.nx || j < 0 || j >= d.ny) {
+    const GhostSrc g = resolve_cell(d, I, J);
+    if (g.post) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) v[k] = T(d.post[k]);
+      return;
+    }
+    i = g.i;
+    j = g.j;
+    flip = g.flip2;
+  }
+  const long long o = (long long)i * d.ld + j;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) v[k] = q[k * d.ps + o];
+  if (flip) v[2] = -v[2];
+}
+
+// Pass 1 of both directions for every tile: q_l, q_r of each face into P1x / P1y.
+// Qin is the pool of the stage input.
+template <class T, bool FAST, bool CHAR, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT) k_staged_pass1(const SolveDesc* __restrict__ solves,
+                                                      const SolveCtl* __restrict__ ctl,
+                                                      const int4* __restrict__ tiles, int ntiles, const T* Qin, T* W,
+                                                      T gamma, T weps) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int4 tl = tiles[t];
+    if (!ctl[tl.x].active) continue;
+    const SolveDesc& d = solves[tl.x];
+    const int nx = d.nx, ny = d.ny, i0 = tl.y, j0 = tl.z;
+    const bool last_r = i0 + TX >= nx, last_c = j0 + TY >= ny;
+    const int xr0 = i0, xr1 = last_r ? nx + 1 : i0 + TX;
+    const int xc0 = j0 == 0 ? -2 : j0, xc1 = last_c ? ny + 2 : j0 + TY;
+    const int yr0 = i0 == 0 ? -2 : i0, yr1 = last_r ? nx + 2 : i0 + TX;
+    const int yc0 = j0, yc1 = last_c ? ny + 1 : j0 + TY;
+    const int nxc = xc1 - xc0, nxf = (xr1 - xr0) * nxc;
+    const int nyc = yc1 - yc0, nyf = (yr1 - yr0) * nyc;
+    const T* q = Qin + d.off;
+    for (int e = threadIdx.x; e < nxf + nyf; e += NT) {
+      T cells[6][4], ql[4], qr[4];
+      if (e < nxf) {
+        const int fi = xr0 + e / nxc, J = xc0 + e % nxc;  // face between padded rows fi+2 and fi+3
+#pragma unroll
+        for (int s = 0; s < 6; ++s) staged_cell(d, q, fi + s, J + 3, cells[s]);
+        pass1_face<T, FAST, false, CHAR>(cells, gamma, ql, qr, weps);
+        T* w = W + d.w_p1x + (long long)fi * d.l_p1x + (J + 2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          w[k * d.s_p1x] = ql[k];
+          w[(4 + k) * d.s_p1x] = qr[k];
+        }
+      } else {
+        const int e2 = e - nxf;
+        const int I = yr0 + e2 / nyc, fj = yc0 + e2 % nyc;  // face between padded columns fj+2 and fj+3
+#pragma unroll
+        for (int s = 0; s < 6; ++s) staged_cell(d, q, I + 3, fj + s, cells[s]);
+        pass1_face<T, FAST, true, CHAR>(cells, gamma, ql, qr, weps);
+        T* w = W + d.w_p1y + (long long)(I + 2) * d.l_p1y + fj;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          w[k * d.s_p1y] = ql[k];
+          w[(4 + k) * d.s_p1y] = qr[k];
+        }
+      }
+    }
+  }
+}
+
+// Pass 2 (Gauss-point WENO of the pass-1 states, Euler fluxes, face averages)
+// and the Riemann solver of every face a tile owns, into Fx / Fy.
+template <class T, bool FAST, bool BLEND, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT) k_staged_pass2(const SolveDesc* __restrict__ solves,
+                                                      const SolveCtl* __restrict__ ctl,
+                                                      const int4* __restrict__ tiles, int ntiles, T* W, T gamma,
+                                                      T weps) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int4 tl = tiles[t];
+    if (!ctl[tl.x].active) continue;
+    const SolveDesc& d = solves[tl.x];
+    const int nx = d.nx, ny = d.ny, i0 = tl.y, j0 = tl.z;
+    const bool last_r = i0 + TX >= nx, last_c = j0 + TY >= ny;
+    const int xr1 = last_r ? nx + 1 : i0 + TX, xc1 = last_c ? ny : j0 + TY;
+    const int yr1 = last_r ? nx : i0 + TX, yc1 = last_c ? ny + 1 : j0 + TY;
+    const int nxc = xc1 - j0, nxf = (xr1 - i0) * nxc;
+    const int nyc = yc1 - j0, nyf = (yr1 - i0) * nyc;
+    for (int e = threadIdx.x; e < nxf + nyf; e += NT) {
+      T ql[4], qr[4], fl[4], fr_[4], a1[4], a2[4], f1[4], f2[4];
+      if (e < nxf) {
+        const int fi = i0 + e / nxc, jj = j0 + e % nxc;
+        // the five transverse pass-1 states J = jj-2 .. jj+2 (columns jj .. jj+4)
+        const T* p = W + d.w_p1x + (long long)fi * d.l_p1x + jj;
+        tile_gq_side<T, FAST>(p, (int)d.s_p1x, 1, weps, a1, a2);
+        euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          fl[k] = T(0.5) * (f1[k] + f2[k]);
+          ql[k] = T(0.5) * (a1[k] + a2[k]);
+        }
+        tile_gq_side<T, FAST>(p + 4 * d.s_p1x, (int)d.s_p1x, 1, weps, a1, a2);
+        euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          fr_[k] = T(0.5) * (f2[k] + f1[k]);
+          qr[k] = T(0.5) * (a1[k] + a2[k]);
+        }
+        tile_face_flux<T, FAST, false, BLEND>(ql, fl, qr, fr_, gamma, W + d.w_fx, (int)d.s_fx, fi * d.ld + jj);
+      } else {
+        const int e2 = e - nxf;
+        const int ii = i0 + e2 / nyc, fj = j0 + e2 % nyc;
+        // the five transverse pass-1 states I = ii-2 .. ii+2 (rows ii .. ii+4)
+        const T* p = W + d.w_p1y + (long long)ii * d.l_p1y + fj;
+        tile_gq_side<T, FAST>(p, (int)d.s_p1y, d.l_p1y, weps, a1, a2);
+        euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          fl[k] = T(0.5) * (f1[k] + f2[k]);
+          ql[k] = T(0.5) * (a1[k] + a2[k]);
+        }
+        tile_gq_side<T, FAST>(p + 4 * d.s_p1y, (int)d.s_p1y, d.l_p1y, weps, a1, a2);
+        euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          fr_[k] = T(0.5) * (f2[k] + f1[k]);
+          qr[k] = T(0.5) * (a1[k] + a2[k]);
+        }
+        tile_face_flux<T, FAST, true, BLEND>(ql, fl, qr, fr_, gamma, W + d.w_fy, (int)d.s_fy, ii * d.l_p1y + fj);
+      }
+    }
+  }
+}
+
+// Sensor blend, flux difference and SSP-RK3 stage combination of every cell
+// (the last part of k_stage_tiles, on the workspace fluxes); stage 3 also
+// reduces the new state's wave speed per solve.  Qs is the pool of the stage
+// input, Qn the step's initial state, Qo the output pool.
+template <class T, bool FAST, bool BLEND, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT) k_staged_residual(const SolveDesc* __restrict__ solves, SolveCtl* ctl,
+                                                         const int4* __restrict__ tiles, int ntiles, const T* W,
+                                                         const T* Qs, const T* Qn, T* Qo, int stage, T gamma,
+                                                         T jp_lo, T jp_hi) {
+  __shared__ double red[NT / 32];
+  const int tid = threadIdx.x;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int4 tl = tiles[t];
+    if (!ctl[tl.x].active) continue;  // uniform across the CTA
+    const SolveDesc& d = solves[tl.x];
+    const int nx = d.nx, ny = d.ny, i0 = tl.y, j0 = tl.z;
+    const double dt = ctl[tl.x].dt;
+    const T* Fx = W + d.w_fx;
+    const T* Fy = W + d.w_fy;
+    const long long fxs = d.s_fx, fys = d.s_fy;
+    const int lx = d.ld, ly = d.l_p1y;
+    double best = 0.0;
+    for (int e = tid; e < TX * TY; e += NT) {
+      const int i = i0 + e / TY, j = j0 + e % TY;
+      if (i >= nx || j >= ny) continue;
+      T wa = T(1.0), wb = T(1.0), va = T(1.0), vb = T(1.0);
+      if constexpr (BLEND) {
+        wa = tile_sensor<T, FAST>(Fx + 8 * fxs, 0, lx, i, j, i, j, nx + 1, ny, jp_lo, jp_hi);
+        wb = tile_sensor<T, FAST>(Fx + 8 * fxs, 0, lx, i + 1, j, i + 1, j, nx + 1, ny, jp_lo, jp_hi);
+        va = tile_sensor<T, FAST>(Fy + 8 * fys, 0, ly, i, j, i, j, nx, ny + 1, jp_lo, jp_hi);
+        vb = tile_sensor<T, FAST>(Fy + 8 * fys, 0, ly, i, j + 1, i, j + 1, nx, ny + 1, jp_lo, jp_hi);
+      }
+      const long long xa = (long long)i * lx + j, xb = xa + lx;
+      const long long ya = (long long)i * ly + j, yb = ya + 1;
+      T L[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        T fxa, fxb, fya, fyb;
+        if constexpr (BLEND) {
+          fxa = wa * Fx[k * fxs + xa] + (T(1.0) - wa) * Fx[(4 + k) * fxs + xa];
+          fxb = wb * Fx[k * fxs + xb] + (T(1.0) - wb) * Fx[(4 + k) * fxs + xb];
+          fya = va * Fy[k * fys + ya] + (T(1.0) - va) * Fy[(4 + k) * fys + ya];
+          fyb = vb * Fy[k * fys + yb] + (T(1.0) - vb) * Fy[(4 + k) * fys + yb];
+        } else {
+          fxa = Fx[k * fxs + xa];
+          fxb = Fx[k * fxs + xb];
+          fya = Fy[k * fys + ya];
+          fyb = Fy[k * fys + yb];
+        }
+        T dfdx, dgdy;
+        if constexpr (FAST) {
+          dfdx = (fxb - fxa) * qrcp<T, FAST>(T(d.dx));
+          dgdy = (fyb - fya) * qrcp<T, FAST>(T(d.dx));
+        } else {
+          dfdx = (fxb - fxa) / T(d.dx);
+          dgdy = (fyb - fya) / T(d.dx);
+        }
+        L[k] = -(dfdx + dgdy);
+      }
+      const long long o = d.off + (long long)i * d.ld + j;
+      T v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const T qs = Qs[k * d.ps + o];
+        if (stage == 1) {
+          v[k] = qs + T(dt) * L[k];
+        } else if (stage == 2) {
+          v[k] = T(0.75) * Qn[k * d.ps + o] + T(0.25) * qs + T(0.25 * dt) * L[k];
+        } else {
+          v[k] = T(1.0 / 3.0) * Qn[k * d.ps + o] + T(2.0 / 3.0) * qs + T((2.0 / 3.0) * dt) * L[k];
+        }
+        Qo[k * d.ps + o] = v[k];
+      }
+      if (stage == 3) {
+        const T r0 = v[0];
+        const T rho = fmax(r0, T(kEps));
+        T uu, vv;
+        if constexpr (FAST) {
+          const T ir = qrcp<T, FAST>(rho);
+          uu = v[1] * ir;
+          vv = v[2] * ir;
+        } else {
+          uu = v[1] / rho;
+          vv = v[2] / rho;
+        }
+        const T pp = fmax((gamma - T(1.0)) * (v[3] - T(0.5) * rho * (uu * uu + vv * vv)), T(kEps));
+        const T rden = r0 != r0 ? r0 : fmax(r0, T(1e-14));  // np.maximum: a NaN density stays NaN
+        const T x = sqrt(qdiv<T, FAST>(gamma * pp, rden)) + sqrt(uu * uu + vv * vv);
+        best = nan_max_b(best, (double)x);
+      }
+    }
+    if (stage == 3) {
+      for (int off = 16; off > 0; off >>= 1) best = nan_max_b(best, __shfl_xor_sync(0xffffffffu, best, off));
+      if ((tid & 31) == 0) red[tid >> 5] = best;
+      __syncthreads();
+      if (tid == 0) {
+        double b = 0.0;
+        for (int w = 0; w < NT / 32; ++w) b = nan_max_b(b, red[w]);
+        atomicMax(&ctl[tl.x].cmax_bits, (unsigned long long)__double_as_longlong(b));
+        if (!(b < INFINITY)) atomicOr(&ctl[tl.x].status, 1);
+      }
+      __syncthreads();
+    }
   }
 }
 

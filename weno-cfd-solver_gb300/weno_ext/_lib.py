@@ -53,6 +53,7 @@ SIGNATURES = {
     "weno_bc_reflecting": (_i, [_vp, _i64, _i64, _i64, _i64, _i64, _i64, _vp]),
     "weno_init_refac": (_i, [_vp, _i64, _i64, _d, _d, _d, ctypes.POINTER(_i64), _vp]),
     "weno_batch_tile_config_count": (_i, []),
+    "weno_batch_bytes_per_cell": (_d, [_i, _i, _i]),
     "weno_batch_create": (_i, [ctypes.POINTER(_vp), _i64, _i, _i, _i, _i, _i, _d, _d, _d, _d, _d, _i, _vp]),
     "weno_batch_destroy": (_i, [_vp]),
     "weno_batch_add": (_i, [_vp, _i64, _i64, _d, _i, _i64, _vp, _d, _i64, _d, _vp, _i64, _i64, _i64, _i64,

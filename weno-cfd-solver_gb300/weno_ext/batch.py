@@ -51,6 +51,15 @@ class Batch:
     def tile_configs():
         return _lib.load().weno_batch_tile_config_count()
 
+    # tile configuration of the staged kernels (three launches per stage, faces in a workspace)
+    STAGED = 4
+
+    @staticmethod
+    def bytes_per_cell(precision=32, force_hlle=False, tile_config=1):
+        """Device bytes one pool cell costs (the three RK pools, plus the staged
+        configuration's share of the face workspace)."""
+        return _lib.load().weno_batch_bytes_per_cell(int(precision), int(bool(force_hlle)), int(tile_config))
+
     def add(self, q, dx, *, t_end=None, max_steps=None, bc="transmissive", bound=0, post=None, cfl=None):
         """Add a solve from its (nx+6, ny+6, C>=4) array (numpy or torch CUDA); returns its slot."""
         torch = self._torch
