@@ -605,7 +605,7 @@ def run_dropin(args):
     return 0
 
 
-def serving_leg(nreq, rate, lo, hi, t_end, budget_gb, fp64_fraction=0.25, slabs=4, max_wait_s=None):
+def serving_leg(nreq, rate, lo, hi, t_end, budget_gb, fp64_fraction=0.25, slabs=4, max_wait_s=None, chunk_ms=25.0):
     """Serving: a seeded Poisson stream of requests (quadrant or oblique-shock initial
     data, FP32 or FP64 tag, seeded t_end) under an HBM budget with continuous batching."""
     import torch
@@ -614,7 +614,8 @@ def serving_leg(nreq, rate, lo, hi, t_end, budget_gb, fp64_fraction=0.25, slabs=
     budget = int(budget_gb * 1e9)
     reqs = serving.poisson_stream(nreq, rate=rate, lo=lo, hi=hi, seed=SEED + 4, fp64_fraction=fp64_fraction,
                                   t_end=t_end, shock_fraction=0.3)
-    srv = serving.Server(budget, slabs=slabs, max_solves=1024, steps_per_iter=8, max_wait_s=max_wait_s)
+    srv = serving.Server(budget, slabs=slabs, max_solves=1024, steps_per_iter=8, max_wait_s=max_wait_s,
+                         chunk_ms=chunk_ms)
     t0 = time.perf_counter()
     srv.serve(reqs, realtime=True)
     wall = time.perf_counter() - t0
@@ -634,7 +635,7 @@ def serving_leg(nreq, rate, lo, hi, t_end, budget_gb, fp64_fraction=0.25, slabs=
             "config": {"workload": f"{nreq} Poisson requests at {rate}/s, edges log-uniform [{lo},{hi}], "
                                    f"t_end~U{tuple(t_end)}, {int(100 * fp64_fraction)}% FP64, 30% oblique shock, "
                                    f"HBM budget {budget / 1e9:.0f} GB in {slabs} slabs",
-                       "steps_per_iteration": 8, "max_wait_s": max_wait_s},
+                       "first_chunk_steps": 8, "chunk_ms": chunk_ms, "max_wait_s": max_wait_s},
             "serving": summ}
 
 
@@ -644,7 +645,8 @@ def run_c4(args):
     t_end = (float(os.environ.get("WENO_C4_TLO", "0.001")), float(os.environ.get("WENO_C4_THI", "0.003")))
     budget = float(os.environ.get("WENO_C4_BUDGET_GB", "150"))
     wait = os.environ.get("WENO_C4_MAX_WAIT")
-    line = serving_leg(args.requests, rate, lo, hi, t_end, budget, max_wait_s=float(wait) if wait else None)
+    line = serving_leg(args.requests, rate, lo, hi, t_end, budget, max_wait_s=float(wait) if wait else None,
+                       chunk_ms=float(os.environ.get("WENO_C4_CHUNK_MS", "25")))
     line.update({"config_name": "c4", "n_gpus": 1, "data": "synthetic"})
     print(json.dumps(line))
     return 0

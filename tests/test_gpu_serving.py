@@ -195,3 +195,20 @@ def test_slabs_follow_the_backlog(wx):
     assert all(r.status == 0 and abs(r.t - r.t_end) < 1e-9 for r in reqs)
     assert srv.conversions >= 1
     assert min(r.admitted for r in reqs[4:]) >= min(r.finished for r in reqs[:4])
+
+
+def test_adaptive_chunks_keep_results(wx):
+    """Chunks sized by measured GPU time (chunk_ms) change only when requests are
+    serviced: every request still reaches its t_end with the result it has alone."""
+    from weno_ext import serving
+    reqs = serving.poisson_stream(10, rate=300.0, lo=24, hi=80, seed=9, fp64_fraction=0.3, t_end=(0.01, 0.03),
+                                  shock_fraction=0.3)
+    srv = serving.Server(8 << 20, slabs=2, max_solves=16, steps_per_iter=2, keep_results=True, chunk_ms=2.0)
+    srv.serve(reqs, realtime=False, max_wall=300)
+    chunks = [sl.chunk for sl in srv.slabs]
+    srv.close()
+    assert all(r.status == 0 and abs(r.t - r.t_end) < 1e-9 for r in reqs)
+    assert any(c > 0 for c in chunks)
+    for r in (reqs[1], reqs[-2]):
+        solo = _alone(wx, r)
+        assert solo.steps == r.steps and np.array_equal(solo.result, r.result)

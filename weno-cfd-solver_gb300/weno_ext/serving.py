@@ -107,7 +107,8 @@ def poisson_stream(n, rate, lo, hi, seed, fp64_fraction=0.25, t_end=(0.1, 0.3), 
 
 
 class _Slab:
-    __slots__ = ("index", "nbytes", "precision", "batch", "active", "inflight", "used", "draining")
+    __slots__ = ("index", "nbytes", "precision", "batch", "active", "inflight", "used", "draining", "chunk",
+                 "t_start", "steps")
 
     def __init__(self, index, nbytes):
         self.index = index
@@ -118,23 +119,34 @@ class _Slab:
         self.inflight = None  # CUDA event of the last enqueued chunk
         self.used = 0  # footprint bytes of the admitted requests
         self.draining = False  # takes no new requests: it is being emptied for the other precision
+        self.chunk = 0  # steps of the next chunk (0: the server's initial chunk)
+        self.t_start = None  # CUDA event at the start of the chunk in flight
+        self.steps = 0  # steps of the chunk in flight
 
-    def fits(self, r):
-        return self.nbytes - self.used >= footprint_bytes(r.nx, r.ny, r.precision)
+    def fits(self, r, need):
+        return self.nbytes - self.used >= need
 
 
 class Server:
     def __init__(self, hbm_budget_bytes, *, slabs=4, max_solves=1024, steps_per_iter=8, cfl=0.5, cons=True,
                  force_hlle=False, jp_cri=(1e4, 1.1e4), tile_config=(1, 1), keep_results=False, max_wait_s=None,
-                 fp64_mode="fast"):
+                 fp64_mode="fast", chunk_ms=None):
         import torch
         self.torch = torch
         self.steps_per_iter = int(steps_per_iter)
+        # chunk_ms: size each slab's chunk of steps to about this much GPU time (measured
+        # on its last chunk), so newly arrived requests wait about that long for a slab
+        # whatever its load; None keeps steps_per_iter steps per chunk.
+        self.chunk_ms = chunk_ms
         self.keep_results = keep_results
         self.max_wait_s = max_wait_s
         self.max_solves = int(max_solves)
         self.fp64_mode = fp64_mode
         self.tile_config = {32: tile_config[0], 64: tile_config[1]}
+        # device bytes per pool cell of each precision's batches, against the 3 x 4
+        # state values per cell that footprint_bytes counts
+        self.scale = {p: Batch.bytes_per_cell(p, force_hlle, self.tile_config[p]) / (12 * (4 if p == 32 else 8))
+                      for p in (32, 64)}
         self.kw = dict(cons=cons, force_hlle=force_hlle, jp_cri=jp_cri, cfl=cfl)
         n = max(1, int(slabs))
         self.slab_bytes = int(hbm_budget_bytes) // n
@@ -170,11 +182,17 @@ class Server:
         self.cancelled.add(rid)
 
     # -- slabs ----------------------------------------------------------------
+    def need(self, r):
+        """Bytes request `r` takes in a slab: its state pools and, for a staged
+        batch, its face workspace."""
+        return int(math.ceil(footprint_bytes(r.nx, r.ny, r.precision) * self.scale[r.precision]))
+
     def _open(self, sl, precision):
-        es = 4 if precision == 32 else 8
         mode = "fast" if precision == 32 else self.fp64_mode
-        sl.batch = Batch(sl.nbytes // (3 * 4 * es), self.max_solves, precision=precision, mode=mode,
-                         tile_config=self.tile_config[precision], **self.kw)
+        cfg = self.tile_config[precision]
+        bpc = Batch.bytes_per_cell(precision, self.kw["force_hlle"], cfg)
+        sl.batch = Batch(int(sl.nbytes // bpc), self.max_solves, precision=precision, mode=mode, tile_config=cfg,
+                         **self.kw)
         sl.precision = precision
 
     def _release(self, sl):
@@ -185,6 +203,7 @@ class Server:
         sl.inflight = None
         sl.used = 0
         sl.draining = False
+        sl.chunk = 0
 
     def _try_add(self, sl, r, now):
         q, dx, bc = r.build()
@@ -194,7 +213,7 @@ class Server:
             return False  # no space (first-fit fragmentation) or no slot in this slab
         r.admitted = now
         sl.active[r.slot] = r
-        sl.used += footprint_bytes(r.nx, r.ny, r.precision)
+        sl.used += self.need(r)
         return True
 
     def _place(self, r, now):
@@ -202,7 +221,8 @@ class Server:
         precision with room is busy, it waits for them (no new slab is opened); else into
         a free slab, or into an idle, empty slab of the other precision, which changes
         precision.  Returns "admitted", "busy" or "full"."""
-        mine = [sl for sl in self.slabs if sl.precision == r.precision and not sl.draining and sl.fits(r)]
+        need = self.need(r)
+        mine = [sl for sl in self.slabs if sl.precision == r.precision and not sl.draining and sl.fits(r, need)]
         for sl in mine:
             if sl.inflight is None and self._try_add(sl, r, now):
                 return "admitted"
@@ -251,7 +271,7 @@ class Server:
         for r in requests:
             if r.precision not in (32, 64):
                 raise ValueError(f"request {r.rid}: precision must be 32 or 64")
-            if footprint_bytes(r.nx, r.ny, r.precision) > self.slab_bytes:
+            if self.need(r) > self.slab_bytes:
                 raise ValueError(f"request {r.rid} ({r.nx}x{r.ny}, FP{r.precision}) exceeds a slab of "
                                  f"{self.slab_bytes} bytes")
         t0 = time.perf_counter()
@@ -268,6 +288,9 @@ class Server:
             # retire on every slab whose chunk is done
             for sl in self.slabs:
                 if sl.inflight is not None and sl.inflight.query():
+                    if self.chunk_ms is not None:
+                        per_step = sl.t_start.elapsed_time(sl.inflight) / max(sl.steps, 1)
+                        sl.chunk = int(min(64, max(1, round(self.chunk_ms / max(per_step, 1e-3)))))
                     sl.inflight = None
                     self._retire(sl, time.perf_counter() - t0)
                 elif sl.inflight is None and any(r.rid in self.cancelled for r in sl.active.values()):
@@ -277,8 +300,13 @@ class Server:
             progressed = False
             for sl in self.slabs:
                 if sl.inflight is None and sl.active:
-                    sl.batch.run(self.steps_per_iter)
-                    ev = torch.cuda.Event()
+                    timing = self.chunk_ms is not None
+                    sl.steps = sl.chunk or self.steps_per_iter
+                    if timing:
+                        sl.t_start = torch.cuda.Event(enable_timing=True)
+                        sl.t_start.record(sl.batch.stream)
+                    sl.batch.run(sl.steps)
+                    ev = torch.cuda.Event(enable_timing=timing)
                     ev.record(sl.batch.stream)
                     sl.inflight = ev
                     progressed = True
@@ -308,7 +336,7 @@ class Server:
                     r.result = pool.state(slot)
                 pool.remove(slot)
                 del sl.active[slot]
-                sl.used -= footprint_bytes(r.nx, r.ny, r.precision)
+                sl.used -= self.need(r)
 
     def close(self):
         for sl in self.slabs:
