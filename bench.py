@@ -357,7 +357,7 @@ def batched_accuracy(nsolves, every=16):
             "reference": "FP64 batch, fast arithmetic (within 1e-10 relative L1 of exact FP64)"}
 
 
-def batched_leg(nsolves, tune=True):
+def batched_leg(nsolves, tune=True, tile_config=None):
     """Batched: independent four-quadrant solves of uneven size (edges log-uniform in
     [64, 1024], aspect <= 4), each with its own dt and t_end ~ U[0.1, 0.3], component
     WENO5 + HLLC (blend thresholds 1e4 / 1.1e4), FP32, CFL 0.5, all advanced together by
@@ -374,7 +374,9 @@ def batched_leg(nsolves, tune=True):
     t_ends = rng.uniform(0.1, 0.3, len(shapes))
     kw = dict(precision=32, mode="fast", cons=True, force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.5)
     sample = states[:: max(1, len(states) // 64)]
-    if tune:
+    if tile_config is not None:
+        cfg, tuning = int(tile_config), None
+    elif tune:
         cfg, tuning = autotune.best_tile_config(sample, **kw)
     else:
         cfg, tuning = 1, None
@@ -439,7 +441,7 @@ def batched_leg(nsolves, tune=True):
 
 
 def run_c3(args):
-    line = batched_leg(args.solves)
+    line = batched_leg(args.solves, tile_config=args.tile_config)
     line.update({"config_name": "c3", "n_gpus": 1, "data": "synthetic"})
     if os.environ.get("WENO_C3_ACCURACY", "1") != "0":
         line["fp32_vs_fp64"] = batched_accuracy(args.solves)
@@ -605,7 +607,8 @@ def run_dropin(args):
     return 0
 
 
-def serving_leg(nreq, rate, lo, hi, t_end, budget_gb, fp64_fraction=0.25, slabs=4, max_wait_s=None, chunk_ms=25.0):
+def serving_leg(nreq, rate, lo, hi, t_end, budget_gb, fp64_fraction=0.25, slabs=4, max_wait_s=None, chunk_ms=25.0,
+                accuracy_sample=8):
     """Serving: a seeded Poisson stream of requests (quadrant or oblique-shock initial
     data, FP32 or FP64 tag, seeded t_end) under an HBM budget with continuous batching."""
     import torch
@@ -614,8 +617,12 @@ def serving_leg(nreq, rate, lo, hi, t_end, budget_gb, fp64_fraction=0.25, slabs=
     budget = int(budget_gb * 1e9)
     reqs = serving.poisson_stream(nreq, rate=rate, lo=lo, hi=hi, seed=SEED + 4, fp64_fraction=fp64_fraction,
                                   t_end=t_end, shock_fraction=0.3)
+    # a seeded sample of FP32 requests keeps its result, to be compared with FP64 runs
+    fp32 = [r.rid for r in reqs if r.precision == 32]
+    sample = set(np.random.default_rng(SEED + 5).choice(fp32, size=min(accuracy_sample, len(fp32)),
+                                                        replace=False).tolist()) if fp32 else set()
     srv = serving.Server(budget, slabs=slabs, max_solves=1024, steps_per_iter=8, max_wait_s=max_wait_s,
-                         chunk_ms=chunk_ms)
+                         chunk_ms=chunk_ms, keep_results=sample)
     t0 = time.perf_counter()
     srv.serve(reqs, realtime=True)
     wall = time.perf_counter() - t0
@@ -623,6 +630,24 @@ def serving_leg(nreq, rate, lo, hi, t_end, budget_gb, fp64_fraction=0.25, slabs=
     srv.close()
     summ = serving.summarize(reqs, wall)
     summ["slab_conversions"] = conversions
+    if sample:
+        # the same requests alone in FP64 (fast arithmetic, within 1e-10 of exact FP64)
+        errs = []
+        for r in reqs:
+            if r.rid not in sample or r.status != 0:
+                continue
+            twin = serving.Request(**{k: getattr(r, k) for k in ("rid", "nx", "ny", "kind", "t_end", "seed", "mach",
+                                                                  "theta")}, arrival=0.0, precision=64)
+            solo = serving.Server(max(int(4e9), 4 * serving.footprint_bytes(r.nx, r.ny, 64) * 8), slabs=1,
+                                  max_solves=2, keep_results=True)
+            solo.serve([twin], realtime=False)
+            solo.close()
+            if twin.status == 0:
+                a, b = r.result[3:-3, 3:-3, 0], twin.result[3:-3, 3:-3, 0]
+                errs.append(float(np.abs(a - b).sum() / np.abs(b).sum()))
+        if errs:
+            summ["fp32_vs_fp64_rho_rel_l1"] = {"requests": len(errs), "median": float(np.median(errs)),
+                                              "max": float(np.max(errs))}
     # work of each request (cells x steps) against its time to solution: the tail is
     # the largest requests, whose work spans more than three decades over [lo, hi]
     work = np.array([r.cells * r.steps for r in reqs if r.status == 0])
@@ -717,6 +742,9 @@ def main():
                          "c2: oblique shock 4096x1024 FP32 vs FP64; c3: batched uneven solves; c4: serving stream; "
                          "dropin: the weno_ext functions themselves (l_local_py & co.)")
     ap.add_argument("--solves", type=int, default=512)
+    ap.add_argument("--tile-config", type=int, default=None,
+                    help="c3: run the batch with this tile configuration instead of the autotuned one "
+                         "(0-3 fused tile kernel, 4 staged kernels)")
     ap.add_argument("--requests", type=int, default=300)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (512 solves) leg of the default line")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream leg of the default line")

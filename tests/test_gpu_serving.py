@@ -189,7 +189,8 @@ def test_slabs_follow_the_backlog(wx):
     reqs += [serving.Request(rid=4 + k, arrival=0.0, nx=40, ny=40, kind="quadrant", precision=64, t_end=0.01,
                              seed=10 + k) for k in range(2)]
     slab = serving.footprint_bytes(40, 40, 64) + 1024  # one FP64 or two FP32 requests per slab
-    srv = serving.Server(2 * slab, slabs=2, max_solves=4, steps_per_iter=2, max_wait_s=0.0)
+    # fused batches for both precisions, so that a request's slab bytes are its state pools
+    srv = serving.Server(2 * slab, slabs=2, max_solves=4, steps_per_iter=2, max_wait_s=0.0, tile_config=(1, 1))
     srv.serve(reqs, realtime=False, max_wall=120)
     srv.close()
     assert all(r.status == 0 and abs(r.t - r.t_end) < 1e-9 for r in reqs)

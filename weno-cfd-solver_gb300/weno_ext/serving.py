@@ -129,7 +129,8 @@ class _Slab:
 
 class Server:
     def __init__(self, hbm_budget_bytes, *, slabs=4, max_solves=1024, steps_per_iter=8, cfl=0.5, cons=True,
-                 force_hlle=False, jp_cri=(1e4, 1.1e4), tile_config=(1, 1), keep_results=False, max_wait_s=None,
+                 force_hlle=False, jp_cri=(1e4, 1.1e4), tile_config=(1, Batch.STAGED), keep_results=False,
+                 max_wait_s=None,
                  fp64_mode="fast", chunk_ms=None):
         import torch
         self.torch = torch
@@ -142,6 +143,9 @@ class Server:
         self.max_wait_s = max_wait_s
         self.max_solves = int(max_solves)
         self.fp64_mode = fp64_mode
+        # tile configuration per precision: the fused tile kernel for FP32, the staged
+        # kernels for FP64 (bound by the FP64 pipe, where recomputing halo faces
+        # costs more than moving the faces through HBM)
         self.tile_config = {32: tile_config[0], 64: tile_config[1]}
         # device bytes per pool cell of each precision's batches, against the 3 x 4
         # state values per cell that footprint_bytes counts
@@ -332,7 +336,8 @@ class Server:
                 inf = pool.info(slot)
                 r.finished, r.steps, r.t = now, inf["steps"], inf["t"]
                 r.status = CANCELLED if (act[slot] and r.rid in self.cancelled) else inf["status"]
-                if self.keep_results:
+                keep = self.keep_results
+                if keep is True or (isinstance(keep, (set, frozenset)) and r.rid in keep):
                     r.result = pool.state(slot)
                 pool.remove(slot)
                 del sl.active[slot]
