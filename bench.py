@@ -357,7 +357,7 @@ def batched_accuracy(nsolves, every=16):
             "reference": "FP64 batch, fast arithmetic (within 1e-10 relative L1 of exact FP64)"}
 
 
-def batched_leg(nsolves, tune=True, tile_config=None):
+def batched_leg(nsolves, tune=True, tile_config=None, precision=32, max_steps=None):
     """Batched: independent four-quadrant solves of uneven size (edges log-uniform in
     [64, 1024], aspect <= 4), each with its own dt and t_end ~ U[0.1, 0.3], component
     WENO5 + HLLC (blend thresholds 1e4 / 1.1e4), FP32, CFL 0.5, all advanced together by
@@ -372,7 +372,7 @@ def batched_leg(nsolves, tune=True, tile_config=None):
     shapes = problems.batch_shapes(nsolves, 64, 1024, SEED + 3)
     states = [(problems.quadrant(nx, ny, seed=SEED + k), 1.0 / max(nx, ny)) for k, (nx, ny) in enumerate(shapes)]
     t_ends = rng.uniform(0.1, 0.3, len(shapes))
-    kw = dict(precision=32, mode="fast", cons=True, force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.5)
+    kw = dict(precision=precision, mode="fast", cons=True, force_hlle=False, jp_cri=(1e4, 1.1e4), cfl=0.5)
     sample = states[:: max(1, len(states) // 64)]
     if tile_config is not None:
         cfg, tuning = int(tile_config), None
@@ -381,13 +381,13 @@ def batched_leg(nsolves, tune=True, tile_config=None):
     else:
         cfg, tuning = 1, None
     cells = sum(nx * ny for nx, ny in shapes)
-    b = weno_ext.Batch(weno_ext.Batch.pool_cells(shapes, 32), len(shapes), tile_config=cfg, **kw)
-    slots = [b.add(q, dx, t_end=float(te)) for (q, dx), te in zip(states, t_ends)]
+    b = weno_ext.Batch(weno_ext.Batch.pool_cells(shapes, precision), len(shapes), tile_config=cfg, **kw)
+    slots = [b.add(q, dx, t_end=float(te), max_steps=max_steps) for (q, dx), te in zip(states, t_ends)]
     ntiles0 = b.stats()["tiles"]
     b.run(1)
     b.synchronize()
     done_before = b.poll()[2].copy()
-    chunk = 20
+    chunk = 20 if max_steps is None else max(1, min(20, max_steps - 1))
     final = {}
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -424,11 +424,13 @@ def batched_leg(nsolves, tune=True, tile_config=None):
     ok = [k for k in range(len(slots)) if k not in set(failed)]
     tt = np.array([final[k][0]["t"] for k in range(len(slots))])
     b.close()
+    pname = "FP32" if precision == 32 else "FP64 (fast arithmetic)"
     return {
-        "metric": "aggregate cell-updates/s, batched uneven four-quadrant solves (FP32)",
-        "value": cu / (ms / 1e3), "unit": UNIT, "dtype": "f32",
+        "metric": f"aggregate cell-updates/s, batched uneven four-quadrant solves ({pname})",
+        "value": cu / (ms / 1e3), "unit": UNIT, "dtype": "f32" if precision == 32 else "f64",
         "config": {"workload": f"{len(shapes)} four-quadrant solves, edges log-uniform [64,1024], aspect<=4, "
-                               "cons-WENO5+GQ+HLLC, FP32, CFL 0.5, t_end~U[0.1,0.3], per-solve dt",
+                               f"cons-WENO5+GQ+HLLC, {pname}, CFL 0.5, t_end~U[0.1,0.3], per-solve dt"
+                               + (f", at most {max_steps} steps per solve" if max_steps else ""),
                    "cells": cells, "tiles": ntiles0, "tile_config": cfg, "autotune": tuning},
         "steady_state": {"ms_per_step": steady_ms / chunk, "cell_updates_per_s": cells * chunk / (steady_ms / 1e3),
                          "note": f"the first {chunk} graph-replayed steps, every solve active"},
@@ -441,9 +443,10 @@ def batched_leg(nsolves, tune=True, tile_config=None):
 
 
 def run_c3(args):
-    line = batched_leg(args.solves, tile_config=args.tile_config)
+    line = batched_leg(args.solves, tile_config=args.tile_config, precision=64 if args.precision == "f64" and
+                       args.c3_precision_given else 32, max_steps=args.c3_steps)
     line.update({"config_name": "c3", "n_gpus": 1, "data": "synthetic"})
-    if os.environ.get("WENO_C3_ACCURACY", "1") != "0":
+    if os.environ.get("WENO_C3_ACCURACY", "1") != "0" and args.c3_steps is None:
         line["fp32_vs_fp64"] = batched_accuracy(args.solves)
     print(json.dumps(line))
     return 0
@@ -742,6 +745,8 @@ def main():
                          "c2: oblique shock 4096x1024 FP32 vs FP64; c3: batched uneven solves; c4: serving stream; "
                          "dropin: the weno_ext functions themselves (l_local_py & co.)")
     ap.add_argument("--solves", type=int, default=512)
+    ap.add_argument("--c3-steps", type=int, default=None,
+                    help="c3: cap every solve at this many steps (short runs for profiling)")
     ap.add_argument("--tile-config", type=int, default=None,
                     help="c3: run the batch with this tile configuration instead of the autotuned one "
                          "(0-3 fused tile kernel, 4 staged kernels)")
@@ -751,6 +756,8 @@ def main():
     ap.add_argument("--no-dropin", action="store_true", help="skip the numpy l_local_py leg of the default line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    # c3 is the FP32 configuration; --precision f64 given explicitly runs the same batch in FP64
+    args.c3_precision_given = any(a == "--precision" or a.startswith("--precision=") for a in sys.argv[1:])
     if args.impl == "reference":
         return run_reference(args)
     if args.config in ("c1", "c2"):

@@ -585,8 +585,42 @@ __global__ void __launch_bounds__(NT) k_staged_pass1(const SolveDesc* __restrict
   }
 }
 
+// FAST double: face-averaged states and fluxes of two neighbouring faces (along
+// the transverse direction) from one side's pass-1 planes: p points at the
+// first of the six transverse values of component 0, ks is the plane stride
+// and ts the transverse stride.  The two faces' Gauss-point reconstructions
+// share their first and second differences (weno5_gq_two).  With `two` false
+// only face A is wanted and the sixth value is not read.
+template <bool Y>
+__device__ __forceinline__ void staged_gq_two(const double* p, long long ks, long long ts, bool two, double gamma,
+                                              double weps, double qA[4], double fA[4], double qB[4], double fB[4]) {
+  double a1A[4], a2A[4], a1B[4], a2B[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double* u = p + k * ks;
+    const double v4 = u[4 * ts];
+    weno5_gq_two<double>(u[0], u[ts], u[2 * ts], u[3 * ts], v4, two ? u[5 * ts] : v4, weps, a1A[k], a2A[k], a1B[k],
+                         a2B[k]);
+  }
+  double f1[4], f2[4];
+  euler_flux_pair<double, true, Y>(a1A, a2A, gamma, f1, f2);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    fA[k] = 0.5 * (f1[k] + f2[k]);
+    qA[k] = 0.5 * (a1A[k] + a2A[k]);
+  }
+  if (!two) return;
+  euler_flux_pair<double, true, Y>(a1B, a2B, gamma, f1, f2);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    fB[k] = 0.5 * (f1[k] + f2[k]);
+    qB[k] = 0.5 * (a1B[k] + a2B[k]);
+  }
+}
+
 // Pass 2 (Gauss-point WENO of the pass-1 states, Euler fluxes, face averages)
-// and the Riemann solver of every face a tile owns, into Fx / Fy.
+// and the Riemann solver of every face a tile owns, into Fx / Fy.  FAST double
+// takes two transverse neighbours per thread (as the single-grid k_pass2_two).
 template <class T, bool FAST, bool BLEND, int TX, int TY, int NT>
 __global__ void __launch_bounds__(NT) k_staged_pass2(const SolveDesc* __restrict__ solves,
                                                       const SolveCtl* __restrict__ ctl,
@@ -602,47 +636,77 @@ __global__ void __launch_bounds__(NT) k_staged_pass2(const SolveDesc* __restrict
     const int yr1 = last_r ? nx : i0 + TX, yc1 = last_c ? ny + 1 : j0 + TY;
     const int nxc = xc1 - j0, nxf = (xr1 - i0) * nxc;
     const int nyc = yc1 - j0, nyf = (yr1 - i0) * nyc;
-    for (int e = threadIdx.x; e < nxf + nyf; e += NT) {
-      T ql[4], qr[4], fl[4], fr_[4], a1[4], a2[4], f1[4], f2[4];
-      if (e < nxf) {
-        const int fi = i0 + e / nxc, jj = j0 + e % nxc;
-        // the five transverse pass-1 states J = jj-2 .. jj+2 (columns jj .. jj+4)
-        const T* p = W + d.w_p1x + (long long)fi * d.l_p1x + jj;
-        tile_gq_side<T, FAST>(p, (int)d.s_p1x, 1, weps, a1, a2);
-        euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          fl[k] = T(0.5) * (f1[k] + f2[k]);
-          ql[k] = T(0.5) * (a1[k] + a2[k]);
+    if constexpr (FAST && is_native_f64<T>) {
+      const int nxp = (nxc + 1) / 2, nxi = (xr1 - i0) * nxp;  // x-face pairs (jj, jj+1)
+      const int nyi = ((yr1 - i0 + 1) / 2) * nyc;              // y-face pairs (ii, ii+1)
+      for (int e = threadIdx.x; e < nxi + nyi; e += NT) {
+        double qlA[4], flA[4], qlB[4], flB[4], qrA[4], frA[4], qrB[4], frB[4];
+        if (e < nxi) {
+          const int fi = i0 + e / nxp, jj = j0 + 2 * (e % nxp);
+          const bool two = jj + 1 < xc1;
+          const double* p = W + d.w_p1x + (long long)fi * d.l_p1x + jj;
+          staged_gq_two<false>(p, d.s_p1x, 1, two, gamma, weps, qlA, flA, qlB, flB);
+          staged_gq_two<false>(p + 4 * d.s_p1x, d.s_p1x, 1, two, gamma, weps, qrA, frA, qrB, frB);
+          tile_face_flux<T, FAST, false, BLEND>(qlA, flA, qrA, frA, gamma, W + d.w_fx, (int)d.s_fx, fi * d.ld + jj);
+          if (two)
+            tile_face_flux<T, FAST, false, BLEND>(qlB, flB, qrB, frB, gamma, W + d.w_fx, (int)d.s_fx,
+                                                  fi * d.ld + jj + 1);
+        } else {
+          const int e2 = e - nxi;
+          const int ii = i0 + 2 * (e2 / nyc), fj = j0 + e2 % nyc;
+          const bool two = ii + 1 < yr1;
+          const double* p = W + d.w_p1y + (long long)ii * d.l_p1y + fj;
+          staged_gq_two<true>(p, d.s_p1y, d.l_p1y, two, gamma, weps, qlA, flA, qlB, flB);
+          staged_gq_two<true>(p + 4 * d.s_p1y, d.s_p1y, d.l_p1y, two, gamma, weps, qrA, frA, qrB, frB);
+          tile_face_flux<T, FAST, true, BLEND>(qlA, flA, qrA, frA, gamma, W + d.w_fy, (int)d.s_fy, ii * d.l_p1y + fj);
+          if (two)
+            tile_face_flux<T, FAST, true, BLEND>(qlB, flB, qrB, frB, gamma, W + d.w_fy, (int)d.s_fy,
+                                                 (ii + 1) * d.l_p1y + fj);
         }
-        tile_gq_side<T, FAST>(p + 4 * d.s_p1x, (int)d.s_p1x, 1, weps, a1, a2);
-        euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
+      }
+    } else {
+      for (int e = threadIdx.x; e < nxf + nyf; e += NT) {
+        T ql[4], qr[4], fl[4], fr_[4], a1[4], a2[4], f1[4], f2[4];
+        if (e < nxf) {
+          const int fi = i0 + e / nxc, jj = j0 + e % nxc;
+          // the five transverse pass-1 states J = jj-2 .. jj+2 (columns jj .. jj+4)
+          const T* p = W + d.w_p1x + (long long)fi * d.l_p1x + jj;
+          tile_gq_side<T, FAST>(p, (int)d.s_p1x, 1, weps, a1, a2);
+          euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          fr_[k] = T(0.5) * (f2[k] + f1[k]);
-          qr[k] = T(0.5) * (a1[k] + a2[k]);
-        }
-        tile_face_flux<T, FAST, false, BLEND>(ql, fl, qr, fr_, gamma, W + d.w_fx, (int)d.s_fx, fi * d.ld + jj);
-      } else {
-        const int e2 = e - nxf;
-        const int ii = i0 + e2 / nyc, fj = j0 + e2 % nyc;
-        // the five transverse pass-1 states I = ii-2 .. ii+2 (rows ii .. ii+4)
-        const T* p = W + d.w_p1y + (long long)ii * d.l_p1y + fj;
-        tile_gq_side<T, FAST>(p, (int)d.s_p1y, d.l_p1y, weps, a1, a2);
-        euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
+          for (int k = 0; k < 4; ++k) {
+            fl[k] = T(0.5) * (f1[k] + f2[k]);
+            ql[k] = T(0.5) * (a1[k] + a2[k]);
+          }
+          tile_gq_side<T, FAST>(p + 4 * d.s_p1x, (int)d.s_p1x, 1, weps, a1, a2);
+          euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          fl[k] = T(0.5) * (f1[k] + f2[k]);
-          ql[k] = T(0.5) * (a1[k] + a2[k]);
-        }
-        tile_gq_side<T, FAST>(p + 4 * d.s_p1y, (int)d.s_p1y, d.l_p1y, weps, a1, a2);
-        euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
+          for (int k = 0; k < 4; ++k) {
+            fr_[k] = T(0.5) * (f2[k] + f1[k]);
+            qr[k] = T(0.5) * (a1[k] + a2[k]);
+          }
+          tile_face_flux<T, FAST, false, BLEND>(ql, fl, qr, fr_, gamma, W + d.w_fx, (int)d.s_fx, fi * d.ld + jj);
+        } else {
+          const int e2 = e - nxf;
+          const int ii = i0 + e2 / nyc, fj = j0 + e2 % nyc;
+          // the five transverse pass-1 states I = ii-2 .. ii+2 (rows ii .. ii+4)
+          const T* p = W + d.w_p1y + (long long)ii * d.l_p1y + fj;
+          tile_gq_side<T, FAST>(p, (int)d.s_p1y, d.l_p1y, weps, a1, a2);
+          euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          fr_[k] = T(0.5) * (f2[k] + f1[k]);
-          qr[k] = T(0.5) * (a1[k] + a2[k]);
+          for (int k = 0; k < 4; ++k) {
+            fl[k] = T(0.5) * (f1[k] + f2[k]);
+            ql[k] = T(0.5) * (a1[k] + a2[k]);
+          }
+          tile_gq_side<T, FAST>(p + 4 * d.s_p1y, (int)d.s_p1y, d.l_p1y, weps, a1, a2);
+          euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            fr_[k] = T(0.5) * (f2[k] + f1[k]);
+            qr[k] = T(0.5) * (a1[k] + a2[k]);
+          }
+          tile_face_flux<T, FAST, true, BLEND>(ql, fl, qr, fr_, gamma, W + d.w_fy, (int)d.s_fy, ii * d.l_p1y + fj);
         }
-        tile_face_flux<T, FAST, true, BLEND>(ql, fl, qr, fr_, gamma, W + d.w_fy, (int)d.s_fy, ii * d.l_p1y + fj);
       }
     }
   }
