@@ -225,7 +225,9 @@ int weno_batch_stats(weno_batch* b, int64_t* ntiles, int64_t* free_cells, int* l
  * tile list holds each added solve's tiles in slot order, rows then columns;
  * grid > 0 fixes the stage kernels' persistent grid (CTA k walks tiles k,
  * k + grid, ...).  tile < 0 restores normal operation (1 s waits, grid from
- * occupancy).  No copy is left in flight and no GPU fault is involved. */
+ * occupancy).  No copy is left in flight and no GPU fault is involved.  The
+ * staged configuration (tile_config 4) stages nothing by TMA: there only the
+ * fixed grid applies. */
 int weno_batch_debug_skip_copy(weno_batch* b, int tile, int64_t wait_ns, int grid);
 
 /* ------------------------------------------------------------------------
