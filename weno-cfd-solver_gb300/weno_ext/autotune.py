@@ -1,13 +1,16 @@
 """Tile-shape autotuner of the batched solver.
 
-The fused stage kernels take their tile shape (TX x TY interior cells per CTA,
-with a 3-cell halo -- 4 with the sensor blend -- staged in shared memory) from
-a small set compiled into the library.  Which one is fastest depends on the
-precision (shared memory per CTA and hence residency), the scheme (register
-pressure of the characteristic projection, the blend's extra halo) and the mix
-of grid sizes (partial tiles at the edges of small grids).  `best_tile_config`
-times every shape on the caller's batch for a few graph-replayed steps and
-caches the winner per (GPU, precision, arithmetic, scheme, size class).
+The batched solver has five compiled tile configurations: four shapes of the
+fused stage kernel (TX x TY interior cells per CTA, with a 3-cell halo -- 4
+with the sensor blend -- staged in shared memory) and the staged kernels
+(three launches per stage, the faces in a device workspace, no halo
+recompute).  Which one is fastest depends on the precision (shared memory per
+CTA and hence residency; in FP64 the staged kernels win, the halo recompute
+costing more than the traffic it saves), the scheme (register pressure of the
+characteristic projection, the blend's extra halo) and the mix of grid sizes
+(partial tiles at the edges of small grids).  `best_tile_config` times every
+configuration on the caller's batch for a few graph-replayed steps and caches
+the winner per (GPU, precision, arithmetic, scheme, size class).
 """
 
 from __future__ import annotations
