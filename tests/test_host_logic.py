@@ -97,3 +97,12 @@ def test_autotune_size_class_and_cache(tmp_path, monkeypatch):
     assert autotune._load() == {"k": {"config": 2}}
     (tmp_path / "tune.json").write_text("not json")
     assert autotune._load() == {}
+
+
+def test_batch_bytes_per_cell():
+    """Memory a pool cell costs: the three RK pools of four planes, plus the staged
+    configuration's workspace share (1.25 x (16 + 2 NF) values, NF = 4 HLLE / 9 blend)."""
+    assert Batch.bytes_per_cell(32, False, 1) == 12 * 4
+    assert Batch.bytes_per_cell(64, True, 0) == 12 * 8
+    assert Batch.bytes_per_cell(64, True, Batch.STAGED) == (12 + 1.25 * 24) * 8
+    assert Batch.bytes_per_cell(64, False, Batch.STAGED) == (12 + 1.25 * 34) * 8
