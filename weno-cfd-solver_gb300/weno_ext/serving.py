@@ -128,10 +128,17 @@ class _Slab:
 
 
 class Server:
+    """Continuous-batching server over an HBM budget of `hbm_budget_bytes` split into
+    `slabs` slabs.  `steps_per_iter`: steps of a slab's first chunk (and of every chunk
+    when `chunk_ms` is None); `tile_config`: the batch configuration of (FP32, FP64)
+    slabs; `keep_results`: True keeps every finished request's array in
+    `Request.result`, a set of request ids keeps those only; `max_wait_s`: the age bound
+    of admission; `fp64_mode`: "fast" or "exact" arithmetic of the FP64 slabs.  The
+    scheme arguments (`cfl`, `cons`, `force_hlle`, `jp_cri`) apply to every request."""
+
     def __init__(self, hbm_budget_bytes, *, slabs=4, max_solves=1024, steps_per_iter=8, cfl=0.5, cons=True,
                  force_hlle=False, jp_cri=(1e4, 1.1e4), tile_config=(1, Batch.STAGED), keep_results=False,
-                 max_wait_s=None,
-                 fp64_mode="fast", chunk_ms=None):
+                 max_wait_s=None, fp64_mode="fast", chunk_ms=None):
         import torch
         self.torch = torch
         self.steps_per_iter = int(steps_per_iter)
@@ -158,7 +165,7 @@ class Server:
         self.cancelled = set()  # request ids to drop (waiting) or stop (active)
         self.conversions = 0  # slabs handed from one precision to the other
 
-    # -- views kept for callers of the two-pool layout -----------------------
+    # -- views by precision ---------------------------------------------------
     @property
     def active(self):
         """{precision: {(slab, slot): request}} of the admitted requests."""
