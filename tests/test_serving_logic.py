@@ -28,6 +28,7 @@ class _Event:
 
 class _Cuda:
     Event = staticmethod(lambda enable_timing=False: _Event())
+    Stream = staticmethod(lambda priority=0: None)
 
 
 class _Torch:

@@ -116,7 +116,12 @@ namespace {
 template <class T, bool FAST>
 cudaError_t enqueue_batch_step(weno_batch* b) {
   using BL = BatchLaunch<T, FAST>;
-  const int grid = b->fixed_grid > 0 ? b->fixed_grid : std::min(b->ntiles, b->sm_count * b->occ);
+  // The fused kernel keeps a persistent grid (its tiles stage through shared
+  // memory sized for the resident CTAs); the staged kernels launch one CTA per
+  // tile, so their CTAs are short and the block scheduler can interleave the
+  // CTAs of other streams (a higher-priority FP32 batch) between them.
+  const int grid = b->fixed_grid > 0 ? b->fixed_grid
+                   : (b->cfg == kStagedConfig ? b->ntiles : std::min(b->ntiles, b->sm_count * b->occ));
   cudaError_t e;
   if ((e = BL::clock(b->d_ctl, b->max_solves, 0, b->stream))) return e;
   if (b->cfg == kStagedConfig) {
