@@ -178,12 +178,14 @@ __device__ __forceinline__ void tile_gq_side(const T* p, int ks, int ts, T weps,
 
 // Riemann solver of one tile face and its store into the face buffer F
 // (HLLE flux planes, or HLLC + HLLE + mean pressure for the sensor blend).
-template <class T, bool FAST, bool Y, bool BLEND>
+// S = 2 (HLLE only): states and fluxes are twice the face averages.
+template <class T, bool FAST, bool Y, bool BLEND, int S = 1>
 __device__ __forceinline__ void tile_face_flux(const T ql[4], const T fl[4], const T qr[4], const T fr[4], T gamma,
                                                T* F, int FN, int e) {
-  const RiemannPre<T, FAST, Y> rp = riemann_pre<T, FAST, Y>(ql, qr, gamma);
+  static_assert(S == 1 || !BLEND, "doubled states feed the HLLE flux only");
+  const RiemannPre<T, FAST, Y> rp = riemann_pre<T, FAST, Y, S>(ql, qr, gamma);
   T H[4];
-  hlle_flux<T, FAST, Y>(rp, ql, fl, qr, fr, H);
+  hlle_flux<T, FAST, Y, S>(rp, ql, fl, qr, fr, H);
   if constexpr (BLEND) {
     T Gc[4];
     hllc_flux<T, FAST, Y>(rp, ql, fl, qr, fr, Gc);
@@ -211,6 +213,7 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
   using G = TileGeom<TX, TY, BLEND>;
   static_assert(G::UC * sizeof(T) % 16 == 0, "box rows must be whole 16-byte units");
   constexpr uint32_t kBoxBytes = (uint32_t)(sizeof(T) * G::U_ELEMS);
+  constexpr int S = FAST && !BLEND ? 2 : 1;  // FAST HLLE takes the Gauss-point sums
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* U = reinterpret_cast<T*>(smem_raw);
   T* P1 = U + G::U_ELEMS;
@@ -320,18 +323,18 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
         euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          fl[k] = T(0.5) * (f1[k] + f2[k]);
-          ql[k] = T(0.5) * (a1[k] + a2[k]);
+          fl[k] = S == 1 ? T(0.5) * (f1[k] + f2[k]) : f1[k] + f2[k];
+          ql[k] = S == 1 ? T(0.5) * (a1[k] + a2[k]) : a1[k] + a2[k];
         }
         tile_gq_side<T, FAST>(P1 + 4 * G::P1 + fr * G::P1XC + fc, G::P1, 1, weps, a1, a2);
         euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          fr_[k] = T(0.5) * (f2[k] + f1[k]);
-          qr[k] = T(0.5) * (a1[k] + a2[k]);
+          fr_[k] = S == 1 ? T(0.5) * (f2[k] + f1[k]) : f2[k] + f1[k];
+          qr[k] = S == 1 ? T(0.5) * (a1[k] + a2[k]) : a1[k] + a2[k];
         }
       }
-      tile_face_flux<T, FAST, false, BLEND>(ql, fl, qr, fr_, gamma, FX, G::FXR * G::FXC, e);
+      tile_face_flux<T, FAST, false, BLEND, S>(ql, fl, qr, fr_, gamma, FX, G::FXR * G::FXC, e);
     }
     __syncthreads();
     // ---- x flux difference of every cell of the tile (sensor blend of the x faces) ----
@@ -393,18 +396,18 @@ __global__ void __launch_bounds__(NT) k_stage_tiles(const SolveDesc* __restrict_
         euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          fl[k] = T(0.5) * (f1[k] + f2[k]);
-          ql[k] = T(0.5) * (a1[k] + a2[k]);
+          fl[k] = S == 1 ? T(0.5) * (f1[k] + f2[k]) : f1[k] + f2[k];
+          ql[k] = S == 1 ? T(0.5) * (a1[k] + a2[k]) : a1[k] + a2[k];
         }
         tile_gq_side<T, FAST>(P1 + 4 * G::P1 + fr * G::P1YC + fc, G::P1, G::P1YC, weps, a1, a2);
         euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          fr_[k] = T(0.5) * (f2[k] + f1[k]);
-          qr[k] = T(0.5) * (a1[k] + a2[k]);
+          fr_[k] = S == 1 ? T(0.5) * (f2[k] + f1[k]) : f2[k] + f1[k];
+          qr[k] = S == 1 ? T(0.5) * (a1[k] + a2[k]) : a1[k] + a2[k];
         }
       }
-      tile_face_flux<T, FAST, true, BLEND>(ql, fl, qr, fr_, gamma, FY, G::FYR * G::FYC, e);
+      tile_face_flux<T, FAST, true, BLEND, S>(ql, fl, qr, fr_, gamma, FY, G::FYR * G::FYC, e);
     }
     __syncthreads();
 
@@ -590,8 +593,9 @@ __global__ void __launch_bounds__(NT) k_staged_pass1(const SolveDesc* __restrict
 // first of the six transverse values of component 0, ks is the plane stride
 // and ts the transverse stride.  The two faces' Gauss-point reconstructions
 // share their first and second differences (weno5_gq_two).  With `two` false
-// only face A is wanted and the sixth value is not read.
-template <bool Y>
+// only face A is wanted and the sixth value is not read.  SUM: twice the
+// averages (the Gauss-point sums), for the doubled-state HLLE.
+template <bool Y, bool SUM>
 __device__ __forceinline__ void staged_gq_two(const double* p, long long ks, long long ts, bool two, double gamma,
                                               double weps, double qA[4], double fA[4], double qB[4], double fB[4]) {
   double a1A[4], a2A[4], a1B[4], a2B[4];
@@ -606,15 +610,15 @@ __device__ __forceinline__ void staged_gq_two(const double* p, long long ks, lon
   euler_flux_pair<double, true, Y>(a1A, a2A, gamma, f1, f2);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    fA[k] = 0.5 * (f1[k] + f2[k]);
-    qA[k] = 0.5 * (a1A[k] + a2A[k]);
+    fA[k] = SUM ? f1[k] + f2[k] : 0.5 * (f1[k] + f2[k]);
+    qA[k] = SUM ? a1A[k] + a2A[k] : 0.5 * (a1A[k] + a2A[k]);
   }
   if (!two) return;
   euler_flux_pair<double, true, Y>(a1B, a2B, gamma, f1, f2);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    fB[k] = 0.5 * (f1[k] + f2[k]);
-    qB[k] = 0.5 * (a1B[k] + a2B[k]);
+    fB[k] = SUM ? f1[k] + f2[k] : 0.5 * (f1[k] + f2[k]);
+    qB[k] = SUM ? a1B[k] + a2B[k] : 0.5 * (a1B[k] + a2B[k]);
   }
 }
 
@@ -637,6 +641,8 @@ __global__ void __launch_bounds__(NT) k_staged_pass2(const SolveDesc* __restrict
     const int nxc = xc1 - j0, nxf = (xr1 - i0) * nxc;
     const int nyc = yc1 - j0, nyf = (yr1 - i0) * nyc;
     if constexpr (FAST && is_native_f64<T>) {
+      constexpr bool SUM = !BLEND;  // the HLLE flux takes the Gauss-point sums
+      constexpr int S = SUM ? 2 : 1;
       const int nxp = (nxc + 1) / 2, nxi = (xr1 - i0) * nxp;  // x-face pairs (jj, jj+1)
       const int nyi = ((yr1 - i0 + 1) / 2) * nyc;              // y-face pairs (ii, ii+1)
       for (int e = threadIdx.x; e < nxi + nyi; e += NT) {
@@ -645,26 +651,30 @@ __global__ void __launch_bounds__(NT) k_staged_pass2(const SolveDesc* __restrict
           const int fi = i0 + e / nxp, jj = j0 + 2 * (e % nxp);
           const bool two = jj + 1 < xc1;
           const double* p = W + d.w_p1x + (long long)fi * d.l_p1x + jj;
-          staged_gq_two<false>(p, d.s_p1x, 1, two, gamma, weps, qlA, flA, qlB, flB);
-          staged_gq_two<false>(p + 4 * d.s_p1x, d.s_p1x, 1, two, gamma, weps, qrA, frA, qrB, frB);
-          tile_face_flux<T, FAST, false, BLEND>(qlA, flA, qrA, frA, gamma, W + d.w_fx, (int)d.s_fx, fi * d.ld + jj);
+          staged_gq_two<false, SUM>(p, d.s_p1x, 1, two, gamma, weps, qlA, flA, qlB, flB);
+          staged_gq_two<false, SUM>(p + 4 * d.s_p1x, d.s_p1x, 1, two, gamma, weps, qrA, frA, qrB, frB);
+          tile_face_flux<T, FAST, false, BLEND, S>(qlA, flA, qrA, frA, gamma, W + d.w_fx, (int)d.s_fx,
+                                                   fi * d.ld + jj);
           if (two)
-            tile_face_flux<T, FAST, false, BLEND>(qlB, flB, qrB, frB, gamma, W + d.w_fx, (int)d.s_fx,
-                                                  fi * d.ld + jj + 1);
+            tile_face_flux<T, FAST, false, BLEND, S>(qlB, flB, qrB, frB, gamma, W + d.w_fx, (int)d.s_fx,
+                                                     fi * d.ld + jj + 1);
         } else {
           const int e2 = e - nxi;
           const int ii = i0 + 2 * (e2 / nyc), fj = j0 + e2 % nyc;
           const bool two = ii + 1 < yr1;
           const double* p = W + d.w_p1y + (long long)ii * d.l_p1y + fj;
-          staged_gq_two<true>(p, d.s_p1y, d.l_p1y, two, gamma, weps, qlA, flA, qlB, flB);
-          staged_gq_two<true>(p + 4 * d.s_p1y, d.s_p1y, d.l_p1y, two, gamma, weps, qrA, frA, qrB, frB);
-          tile_face_flux<T, FAST, true, BLEND>(qlA, flA, qrA, frA, gamma, W + d.w_fy, (int)d.s_fy, ii * d.l_p1y + fj);
+          staged_gq_two<true, SUM>(p, d.s_p1y, d.l_p1y, two, gamma, weps, qlA, flA, qlB, flB);
+          staged_gq_two<true, SUM>(p + 4 * d.s_p1y, d.s_p1y, d.l_p1y, two, gamma, weps, qrA, frA, qrB, frB);
+          tile_face_flux<T, FAST, true, BLEND, S>(qlA, flA, qrA, frA, gamma, W + d.w_fy, (int)d.s_fy,
+                                                  ii * d.l_p1y + fj);
           if (two)
-            tile_face_flux<T, FAST, true, BLEND>(qlB, flB, qrB, frB, gamma, W + d.w_fy, (int)d.s_fy,
-                                                 (ii + 1) * d.l_p1y + fj);
+            tile_face_flux<T, FAST, true, BLEND, S>(qlB, flB, qrB, frB, gamma, W + d.w_fy, (int)d.s_fy,
+                                                    (ii + 1) * d.l_p1y + fj);
         }
       }
     } else {
+      // FAST HLLE takes the Gauss-point sums (twice the face averages)
+      constexpr int S = FAST && !BLEND ? 2 : 1;
       for (int e = threadIdx.x; e < nxf + nyf; e += NT) {
         T ql[4], qr[4], fl[4], fr_[4], a1[4], a2[4], f1[4], f2[4];
         if (e < nxf) {
@@ -675,17 +685,17 @@ __global__ void __launch_bounds__(NT) k_staged_pass2(const SolveDesc* __restrict
           euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            fl[k] = T(0.5) * (f1[k] + f2[k]);
-            ql[k] = T(0.5) * (a1[k] + a2[k]);
+            fl[k] = S == 1 ? T(0.5) * (f1[k] + f2[k]) : f1[k] + f2[k];
+            ql[k] = S == 1 ? T(0.5) * (a1[k] + a2[k]) : a1[k] + a2[k];
           }
           tile_gq_side<T, FAST>(p + 4 * d.s_p1x, (int)d.s_p1x, 1, weps, a1, a2);
           euler_flux_pair<T, FAST, false>(a1, a2, gamma, f1, f2);
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            fr_[k] = T(0.5) * (f2[k] + f1[k]);
-            qr[k] = T(0.5) * (a1[k] + a2[k]);
+            fr_[k] = S == 1 ? T(0.5) * (f2[k] + f1[k]) : f2[k] + f1[k];
+            qr[k] = S == 1 ? T(0.5) * (a1[k] + a2[k]) : a1[k] + a2[k];
           }
-          tile_face_flux<T, FAST, false, BLEND>(ql, fl, qr, fr_, gamma, W + d.w_fx, (int)d.s_fx, fi * d.ld + jj);
+          tile_face_flux<T, FAST, false, BLEND, S>(ql, fl, qr, fr_, gamma, W + d.w_fx, (int)d.s_fx, fi * d.ld + jj);
         } else {
           const int e2 = e - nxf;
           const int ii = i0 + e2 / nyc, fj = j0 + e2 % nyc;
@@ -695,17 +705,17 @@ __global__ void __launch_bounds__(NT) k_staged_pass2(const SolveDesc* __restrict
           euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            fl[k] = T(0.5) * (f1[k] + f2[k]);
-            ql[k] = T(0.5) * (a1[k] + a2[k]);
+            fl[k] = S == 1 ? T(0.5) * (f1[k] + f2[k]) : f1[k] + f2[k];
+            ql[k] = S == 1 ? T(0.5) * (a1[k] + a2[k]) : a1[k] + a2[k];
           }
           tile_gq_side<T, FAST>(p + 4 * d.s_p1y, (int)d.s_p1y, d.l_p1y, weps, a1, a2);
           euler_flux_pair<T, FAST, true>(a1, a2, gamma, f1, f2);
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            fr_[k] = T(0.5) * (f2[k] + f1[k]);
-            qr[k] = T(0.5) * (a1[k] + a2[k]);
+            fr_[k] = S == 1 ? T(0.5) * (f2[k] + f1[k]) : f2[k] + f1[k];
+            qr[k] = S == 1 ? T(0.5) * (a1[k] + a2[k]) : a1[k] + a2[k];
           }
-          tile_face_flux<T, FAST, true, BLEND>(ql, fl, qr, fr_, gamma, W + d.w_fy, (int)d.s_fy, ii * d.l_p1y + fj);
+          tile_face_flux<T, FAST, true, BLEND, S>(ql, fl, qr, fr_, gamma, W + d.w_fy, (int)d.s_fy, ii * d.l_p1y + fj);
         }
       }
     }

@@ -318,20 +318,20 @@ __device__ __forceinline__ void weno_nd(double e0, double e1, double e2, double 
   den = (c0 + c1 + c2) * scale;
 }
 
-// x = a/(k b) and y = c/(k d) with one divide, 1/(k b d), when b d is a normal number
-// well inside the double range (tested on its exponent bits, no FP64 slot);
-// otherwise two divides.
+// x = x0 + a/(k b) and y = y0 + c/(k d) with one divide, 1/(k b d), when b d is
+// a normal number well inside the double range (tested on its exponent bits, no
+// FP64 slot); otherwise two divides.
 __device__ __forceinline__ void div_pair(double a, double b, double c, double d, double& x, double& y,
-                                         double k = 1.0) {
+                                         double k = 1.0, double x0 = 0.0, double y0 = 0.0) {
   const double bd = b * d;
   const int e = (__double2hiint(bd) >> 20) & 0x7ff;
   if (e > 64 && e < 1983) {
     const double inv = f64fast::rcp(bd * k);
-    x = a * d * inv;
-    y = c * b * inv;
+    x = fma(a * d, inv, x0);
+    y = fma(c * b, inv, y0);
   } else {
-    x = a / (b * k);
-    y = c / (d * k);
+    x = x0 + a / (b * k);
+    y = y0 + c / (d * k);
   }
 }
 
@@ -383,37 +383,40 @@ __device__ __forceinline__ void weno5_lr_fast(T u0, T u1, T u2, T u3, T u4, T u5
   const T sr0 = d4 - T(3.0) * d3, sr1 = d2 + d3, sr2 = T(3.0) * d2 - d1;  // right: stencils 3-5, 2-4, 1-3
   const T el0 = sl0 * sl0 + C3, el1 = sl1 * sl1 + C2, el2 = sl2 * sl2 + C1;
   const T er0 = sr0 * sr0 + C4, er1 = sr1 * sr1 + C3, er2 = sr2 * sr2 + C2;
-  // candidate polynomials (x6): the right stencil's p1, p2 are the left's p0, p1
-  const T pl0 = -u4 + T(5.0) * u3 + T(2.0) * u2, pl1 = -u1 + T(5.0) * u2 + T(2.0) * u3;
-  const T pl2 = T(2.0) * u0 - T(7.0) * u1 + T(11.0) * u2, pr0 = T(2.0) * u5 - T(7.0) * u4 + T(11.0) * u3;
+  // Candidate polynomials (x6) less six times the centre value, from the same
+  // differences: left 6 u2 + (4 d2 - d3, d1 + 2 d2, 5 d1 - 2 d0), right 6 u3 +
+  // (d1 - 4 d2, -(2 d2 + d3), 2 d4 - 5 d3); each face state is its centre value
+  // plus the weighted slope / 6 (no 6 u2 formed and cancelled).
+  const T gl0 = d2 - sl0, gl1 = sl1 + d2, gl2 = T(2.0) * sl2 - d1;
+  const T gr2 = -d2 - sr2, gr1 = -d2 - sr1, gr0 = T(2.0) * sr0 + d3;
   // The right reconstruction takes its stencils in the mirror order of the left
   // one (1-3, 2-4, 3-5 against 2-4, 1-3, 0-2), so that for mirror-image inputs
-  // (u_k -> u_{5-k}, as across a reflecting wall) it performs the left one's
-  // operations on bit-identical values and the two face states are exact
-  // mirrors, as in the reference's arithmetic.
+  // (u_k -> u_{5-k}, as across a reflecting wall: d_m -> -d_{4-m}) it performs
+  // the left one's operations on bit-identical values and the two face states
+  // are exact mirrors, as in the reference's arithmetic.
   if constexpr (is_native_f64<T>) {
     // linear weights scaled by 10 -- (3, 6, 1) -- and the 1/6 of the candidate
     // polynomials applied once to the shared divide
     double nl, dl, nr, dr;
-    weno_nd(el0, el1, el2, 3.0, 6.0, 1.0, pl0, pl1, pl2, 1.0, nl, dl);
-    weno_nd(er2, er1, er0, 3.0, 6.0, 1.0, pl1, pl0, pr0, 1.0, nr, dr);
-    div_pair(nl, dl, nr, dr, left, right, 6.0);
+    weno_nd(el0, el1, el2, 3.0, 6.0, 1.0, gl0, gl1, gl2, 1.0, nl, dl);
+    weno_nd(er2, er1, er0, 3.0, 6.0, 1.0, gr2, gr1, gr0, 1.0, nr, dr);
+    div_pair(nl, dl, nr, dr, left, right, 6.0, u2, u3);
   } else {
-    left = weno_combine<T, true>(el0, el1, el2, T(0.3), T(0.6), T(0.1), pl0, pl1, pl2, T(6.0));
-    right = weno_combine<T, true>(er2, er1, er0, T(0.3), T(0.6), T(0.1), pl1, pl0, pr0, T(6.0));
+    left = u2 + weno_combine<T, true>(el0, el1, el2, T(0.3), T(0.6), T(0.1), gl0, gl1, gl2, T(6.0));
+    right = u3 + weno_combine<T, true>(er2, er1, er0, T(0.3), T(0.6), T(0.1), gr2, gr1, gr0, T(6.0));
   }
 }
 
 // FAST float: the four fields' left/right reconstructions as two packed pairs
-// (fields 0,1 and 2,3) on the FP32x2 instructions.
+// (fields 0,1 and 2,3) on the FP32x2 instructions; field 2 takes weps2.
 __device__ __forceinline__ void weno5_lr_fast_f32_pairs(const float c[6][4], float weps, float left[4],
-                                                        float right[4]) {
+                                                        float right[4], float weps2) {
 #pragma unroll
   for (int f = 0; f < 4; f += 2) {
     f32x2 l, r;
     weno5_lr_fast<f32x2>(f32x2(c[0][f], c[0][f + 1]), f32x2(c[1][f], c[1][f + 1]), f32x2(c[2][f], c[2][f + 1]),
                          f32x2(c[3][f], c[3][f + 1]), f32x2(c[4][f], c[4][f + 1]), f32x2(c[5][f], c[5][f + 1]),
-                         f32x2(weps), l, r);
+                         f == 0 ? f32x2(weps) : f32x2(weps2, weps), l, r);
     left[f] = l.v.x;
     left[f + 1] = l.v.y;
     right[f] = r.v.x;
@@ -519,10 +522,9 @@ __device__ __forceinline__ void roe_avg(const T ul[4], const T ur[4], T gamma, T
     const T rl = frsqrt(rho_l), rr = frsqrt(rho_r);
     const T sqrt_l = rho_l * rl, sqrt_r = rho_r * rr;
     const T il = rl * rl, ir = rr * rr;
-    const T u_l = ul[1] * il, v_l = ul[2] * il;
-    const T u_r = ur[1] * ir, v_r = ur[2] * ir;
-    const T p_l = vmax((gamma - T(1.0)) * (ul[3] - half_rho_speed2<T, FAST>(rho_l, ul[1], ul[2], u_l, v_l)), T(kEps));
-    const T p_r = vmax((gamma - T(1.0)) * (ur[3] - half_rho_speed2<T, FAST>(rho_r, ur[1], ur[2], u_r, v_r)), T(kEps));
+    // kinetic energy (m^2 + n^2) / (2 rho): the velocities themselves are not needed
+    const T p_l = vmax((gamma - T(1.0)) * (ul[3] - T(0.5) * ((ul[1] * ul[1] + ul[2] * ul[2]) * il)), T(kEps));
+    const T p_r = vmax((gamma - T(1.0)) * (ur[3] - T(0.5) * ((ur[1] * ur[1] + ur[2] * ur[2]) * ir)), T(kEps));
     const T id = qrcp<T, FAST>(sqrt_l + sqrt_r);
     u_roe = (ul[1] * rl + ur[1] * rr) * id;
     v_roe = (ul[2] * rl + ur[2] * rr) * id;
@@ -623,20 +625,25 @@ __device__ __forceinline__ void mat4_vec4(const T M[4][4], const T x[4], T out[4
 //   L q = ( G Z/2 + (b q0 - hr q_n),  q0 - G Z,  (q_t - u_t q0)/rho,  G Z/2 - (b q0 - hr q_n) )
 // (n the normal and t the tangential momentum index), and with s = w0+w1+w3:
 //   R w = ( s,  u s + [c (w3-w0) | rho w2],  v s + [rho w2 | c (w3-w0)],  R3 . w ).
+// The shear field is carried as rho w2 = q_t - u_t q0: WENO5 is homogeneous
+// when its epsilon scales with the square of the field (the indicators are
+// quadratic, the candidates linear), so reconstructing rho w2 with
+// eps rho^2 gives rho times the reconstruction of w2, which is what R needs;
+// the 1/rho of L and the rho of R drop out.
 template <class T>
 struct CharScalars {
-  T u, v, c, rho, irho, kin, G, G2, b, hr, h;
+  T u, v, c, rho, kin, G, G2, b, hr, h;
 };
 
 template <class T, bool Y>
 __device__ __forceinline__ void project_left(const CharScalars<T>& k, const T q[4], T w[4]) {
-  const T Z = k.kin * q[0] - k.u * q[1] - k.v * q[2] + q[3];
-  const T X = k.G2 * Z;
+  // Z from q3 upwards and G Z / 2 +- Yv as one FMA each: nine operations
+  const T Z = (k.kin * q[0] + q[3]) - k.u * q[1] - k.v * q[2];
   const T Yv = k.b * q[0] - k.hr * q[Y ? 2 : 1];
-  w[0] = X + Yv;
+  w[0] = k.G2 * Z + Yv;
   w[1] = q[0] - k.G * Z;
-  w[2] = k.irho * (q[Y ? 1 : 2] - (Y ? k.u : k.v) * q[0]);
-  w[3] = X - Yv;
+  w[2] = q[Y ? 1 : 2] - (Y ? k.u : k.v) * q[0];  // rho w2
+  w[3] = k.G2 * Z - Yv;
 }
 template <class T, bool Y>
 __device__ __forceinline__ void project_right(const CharScalars<T>& k, const T w[4], T out[4]) {
@@ -646,12 +653,12 @@ __device__ __forceinline__ void project_right(const CharScalars<T>& k, const T w
   out[0] = s;
   if constexpr (!Y) {
     out[1] = k.u * s + k.c * d;
-    out[2] = k.v * s + k.rho * w[2];
+    out[2] = k.v * s + w[2];
   } else {
-    out[1] = k.u * s + k.rho * w[2];
+    out[1] = k.u * s + w[2];
     out[2] = k.v * s + k.c * d;
   }
-  out[3] = (k.h - un * k.c) * w[0] + k.kin * w[1] + (k.rho * (Y ? k.u : k.v)) * w[2] + (k.h + un * k.c) * w[3];
+  out[3] = (k.h - un * k.c) * w[0] + k.kin * w[1] + (Y ? k.u : k.v) * w[2] + (k.h + un * k.c) * w[3];
 }
 
 // weno.rs:312-315 pressure ; weno.rs:327-352 Zhang-Shu limiter toward `ub`.
@@ -692,7 +699,7 @@ __device__ __forceinline__ void pp_limit(T q[4], const T ub[4], T gamma) {
 template <class T, bool FAST, bool Y, bool CHAR>
 __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T qr[4], T weps) {
   if constexpr (!CHAR && FAST && is_f32<T>) {
-    weno5_lr_fast_f32_pairs(c, weps, ql, qr);
+    weno5_lr_fast_f32_pairs(c, weps, ql, qr, weps);
   } else if constexpr (!CHAR) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -717,21 +724,23 @@ __device__ __forceinline__ void pass1_face(const T c[6][4], T gamma, T ql[4], T 
       k.v = v_a;
       k.c = c_a;
       k.rho = rho_a;
-      k.irho = irho_a;
       k.h = h_a;
       k.kin = T(0.5) * (u_a * u_a + v_a * v_a);
       k.G = (gamma - T(1.0)) * (ic_a * ic_a);
       k.G2 = T(0.5) * k.G;
-      k.b = T(0.5) * (Y ? v_a : u_a) * ic_a;
-      k.hr = T(0.5) * (ic_a * irho_a);
+      const T ich = T(0.5) * ic_a;
+      k.b = (Y ? v_a : u_a) * ich;
+      k.hr = ich * irho_a;
 #pragma unroll
       for (int s = 0; s < 6; ++s) project_left<T, Y>(k, c[s], w[s]);
+      const T weps2 = weps * (rho_a * rho_a);  // epsilon of the shear field rho w2
       if constexpr (is_f32<T>) {
-        weno5_lr_fast_f32_pairs(w, weps, chl, chr);
+        weno5_lr_fast_f32_pairs(w, weps, chl, chr, weps2);
       } else {
 #pragma unroll
         for (int f = 0; f < 4; ++f)
-          weno5_lr_fast<T>(w[0][f], w[1][f], w[2][f], w[3][f], w[4][f], w[5][f], weps, chl[f], chr[f]);
+          weno5_lr_fast<T>(w[0][f], w[1][f], w[2][f], w[3][f], w[4][f], w[5][f], f == 2 ? weps2 : weps, chl[f],
+                           chr[f]);
       }
       project_right<T, Y>(k, chl, ql);
       project_right<T, Y>(k, chr, qr);
@@ -764,11 +773,16 @@ struct RiemannPre {
   T ql0, qr0, u_l, v_l, u_r, v_r, p_l, p_r, s_l, s_r, un_l, un_r;
 };
 
-template <class T, bool FAST, bool Y>
+// S = 2 (FAST): ql, qr are twice the face states (the sums of the two Gauss-point
+// values, which saves the halving multiplies); the clamps then take 2 eps, so
+// densities and pressures are exactly twice the clamped values and every
+// velocity, enthalpy and wave speed is a ratio that the factor leaves alone.
+template <class T, bool FAST, bool Y, int S = 1>
 __device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], const T qr[4], T gamma) {
+  static_assert(S == 1 || FAST, "doubled states are a FAST form");
   RiemannPre<T, FAST, Y> r;
-  r.ql0 = cmax<T, FAST>(ql[0], T(kEps));
-  r.qr0 = cmax<T, FAST>(qr[0], T(kEps));
+  r.ql0 = cmax<T, FAST>(ql[0], T(kEps * S));
+  r.qr0 = cmax<T, FAST>(qr[0], T(kEps * S));
   T h_l, h_r, u_t, v_t, h_t;
   T rsl = T(0.0), rsr = T(0.0);  // FAST: 1/sqrt(rho) per side
   if constexpr (!FAST) {
@@ -781,11 +795,17 @@ __device__ __forceinline__ RiemannPre<T, FAST, Y> riemann_pre(const T ql[4], con
     r.u_l = ql[1] * il; r.v_l = ql[2] * il;
     r.u_r = qr[1] * ir; r.v_r = qr[2] * ir;
   }
-  // FAST: sqrt(rho)*u = q1/sqrt(rho) and sqrt(rho)*h = (E+p)/sqrt(rho).
-  r.p_l = (gamma - T(1.0)) * (ql[3] - half_rho_speed2<T, FAST>(r.ql0, ql[1], ql[2], r.u_l, r.v_l));
-  r.p_r = (gamma - T(1.0)) * (qr[3] - half_rho_speed2<T, FAST>(r.qr0, qr[1], qr[2], r.u_r, r.v_r));
-  r.p_l = cmax<T, FAST>(r.p_l, T(kEps));
-  r.p_r = cmax<T, FAST>(r.p_r, T(kEps));
+  // FAST: sqrt(rho)*u = q1/sqrt(rho) and sqrt(rho)*h = (E+p)/sqrt(rho); the
+  // kinetic energy is (m^2 + n^2) / (2 rho), without the velocities.
+  if constexpr (!FAST) {
+    r.p_l = (gamma - T(1.0)) * (ql[3] - half_rho_speed2<T, FAST>(r.ql0, ql[1], ql[2], r.u_l, r.v_l));
+    r.p_r = (gamma - T(1.0)) * (qr[3] - half_rho_speed2<T, FAST>(r.qr0, qr[1], qr[2], r.u_r, r.v_r));
+  } else {
+    r.p_l = (gamma - T(1.0)) * (ql[3] - T(0.5) * ((ql[1] * ql[1] + ql[2] * ql[2]) * (rsl * rsl)));
+    r.p_r = (gamma - T(1.0)) * (qr[3] - T(0.5) * ((qr[1] * qr[1] + qr[2] * qr[2]) * (rsr * rsr)));
+  }
+  r.p_l = cmax<T, FAST>(r.p_l, T(kEps * S));
+  r.p_r = cmax<T, FAST>(r.p_r, T(kEps * S));
   if constexpr (!FAST) {
     const T srl = sqrt(r.ql0), srr = sqrt(r.qr0);
     const T denom_r = srl + srr;
@@ -822,17 +842,18 @@ __device__ __forceinline__ T guard_denom(T d) {
   return d;
 }
 
-// riemann.rs:191-349 HLLE
-template <class T, bool FAST, bool Y>
+// riemann.rs:191-349 HLLE.  S = 2: states and fluxes are doubled (riemann_pre),
+// the flux is halved on the way out.
+template <class T, bool FAST, bool Y, int S = 1>
 __device__ __forceinline__ void hlle_flux(const RiemannPre<T, FAST, Y>& r, const T ql[4], const T fl[4],
                                           const T qr[4], const T fr[4], T F[4]) {
   const T denom = guard_denom<T, FAST>(r.s_r - r.s_l);
   if (r.s_l >= T(0.0)) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) F[k] = fl[k];
+    for (int k = 0; k < 4; ++k) F[k] = S == 1 ? fl[k] : T(0.5) * fl[k];
   } else if (r.s_r < T(0.0)) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) F[k] = fr[k];
+    for (int k = 0; k < 4; ++k) F[k] = S == 1 ? fr[k] : T(0.5) * fr[k];
   } else {
     const T qlv[4] = {r.ql0, ql[1], ql[2], ql[3]};
     const T qrv[4] = {r.qr0, qr[1], qr[2], qr[3]};
@@ -841,7 +862,7 @@ __device__ __forceinline__ void hlle_flux(const RiemannPre<T, FAST, Y>& r, const
 #pragma unroll
       for (int k = 0; k < 4; ++k) F[k] = (r.s_r * fl[k] - r.s_l * fr[k] + srsl * (qrv[k] - qlv[k])) / denom;
     } else {
-      const T id = qrcp<T, FAST>(denom);
+      const T id = qrcp<T, FAST>(S == 1 ? denom : T(S) * denom);
 #pragma unroll
       for (int k = 0; k < 4; ++k) F[k] = (r.s_r * fl[k] - r.s_l * fr[k] + srsl * (qrv[k] - qlv[k])) * id;
     }

@@ -118,9 +118,11 @@ __device__ __forceinline__ void gq_face(const Planes<T>& P, int64_t row, int64_t
 }
 
 // The Riemann solver and the stores of one pass-2 face (row, col).
-template <class T, bool FAST, bool Y, int OUT>
+// S = 2 (FAST, P2_HLLE): the states and fluxes are twice the face averages.
+template <class T, bool FAST, bool Y, int OUT, int S = 1>
 __device__ __forceinline__ void pass2_emit(const T ql[4], const T fl[4], const T qr[4], const T fr[4], T gamma,
                                            const Pass2Dst& dst, int64_t row, int64_t col, int64_t cols) {
+  static_assert(S == 1 || OUT == P2_HLLE, "doubled states feed the HLLE flux only");
   const int64_t e = row * dst.ld + col;
   if constexpr (OUT == P2_STATES) {
     const int64_t o = (row * cols + col) * 4;
@@ -132,9 +134,9 @@ __device__ __forceinline__ void pass2_emit(const T ql[4], const T fl[4], const T
       static_cast<T*>(dst.d)[o + k] = fr[k];
     }
   } else {
-    const RiemannPre<T, FAST, Y> r = riemann_pre<T, FAST, Y>(ql, qr, gamma);
+    const RiemannPre<T, FAST, Y> r = riemann_pre<T, FAST, Y, S>(ql, qr, gamma);
     T F[4];
-    hlle_flux<T, FAST, Y>(r, ql, fl, qr, fr, F);
+    hlle_flux<T, FAST, Y, S>(r, ql, fl, qr, fr, F);
     if constexpr (OUT == P2_HLLE) {
 #pragma unroll
       for (int k = 0; k < 4; ++k) static_cast<T*>(dst.a)[k * dst.ps + e] = F[k];
@@ -181,8 +183,9 @@ __global__ void __launch_bounds__(128) k_pass2(Planes<T> PL, Planes<T> PR, int64
 }
 
 // Face-averaged states and fluxes of two neighbouring faces (along the
-// transverse direction) from one side's pass-1 planes, FAST arithmetic.
-template <class T, bool Y>
+// transverse direction) from one side's pass-1 planes, FAST arithmetic.  SUM:
+// twice the averages (the Gauss-point sums), for the doubled-state HLLE.
+template <class T, bool Y, bool SUM = false>
 __device__ __forceinline__ void gq_side_two(const Planes<T>& P, int64_t row, int64_t col, T gamma, T weps, T qA[4],
                                             T fA[4], T qB[4], T fB[4]) {
   T a1A[4], a2A[4], a1B[4], a2B[4];
@@ -209,18 +212,19 @@ __device__ __forceinline__ void gq_side_two(const Planes<T>& P, int64_t row, int
       weno5_gq_two<T>(v[0], v[1], v[2], v[3], v[4], v[5], weps, a1A[k], a2A[k], a1B[k], a2B[k]);
     }
   }
+  const T h = SUM ? T(1.0) : T(0.5);
   T f1[4], f2[4];
   euler_flux_pair<T, true, Y>(a1A, a2A, gamma, f1, f2);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    fA[k] = T(0.5) * (f1[k] + f2[k]);
-    qA[k] = T(0.5) * (a1A[k] + a2A[k]);
+    fA[k] = SUM ? f1[k] + f2[k] : h * (f1[k] + f2[k]);
+    qA[k] = SUM ? a1A[k] + a2A[k] : h * (a1A[k] + a2A[k]);
   }
   euler_flux_pair<T, true, Y>(a1B, a2B, gamma, f1, f2);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    fB[k] = T(0.5) * (f1[k] + f2[k]);
-    qB[k] = T(0.5) * (a1B[k] + a2B[k]);
+    fB[k] = SUM ? f1[k] + f2[k] : h * (f1[k] + f2[k]);
+    qB[k] = SUM ? a1B[k] + a2B[k] : h * (a1B[k] + a2B[k]);
   }
 }
 
@@ -237,11 +241,15 @@ __global__ void __launch_bounds__(128) k_pass2_two(Planes<T> PL, Planes<T> PR, i
   else col *= 2;
   if (row >= rows || col >= cols) return;
   const bool two = Y ? (row + 1 < rows) : (col + 1 < cols);
+  // the HLLE flux takes the Gauss-point sums (twice the face averages)
+  constexpr bool SUM = OUT == P2_HLLE;
+  constexpr int S = SUM ? 2 : 1;
   T qlA[4], flA[4], qlB[4], flB[4], qrA[4], frA[4], qrB[4], frB[4];
-  gq_side_two<T, Y>(PL, row, col, gamma, weps, qlA, flA, qlB, flB);
-  gq_side_two<T, Y>(PR, row, col, gamma, weps, qrA, frA, qrB, frB);
-  pass2_emit<T, true, Y, OUT>(qlA, flA, qrA, frA, gamma, dst, row, col, cols);
-  if (two) pass2_emit<T, true, Y, OUT>(qlB, flB, qrB, frB, gamma, dst, Y ? row + 1 : row, Y ? col : col + 1, cols);
+  gq_side_two<T, Y, SUM>(PL, row, col, gamma, weps, qlA, flA, qlB, flB);
+  gq_side_two<T, Y, SUM>(PR, row, col, gamma, weps, qrA, frA, qrB, frB);
+  pass2_emit<T, true, Y, OUT, S>(qlA, flA, qrA, frA, gamma, dst, row, col, cols);
+  if (two)
+    pass2_emit<T, true, Y, OUT, S>(qlB, flB, qrB, frB, gamma, dst, Y ? row + 1 : row, Y ? col : col + 1, cols);
 }
 
 // Riemann solver on caller-provided dense (rows, cols, 4) face arrays
