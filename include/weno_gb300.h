@@ -271,8 +271,10 @@ int weno_probe_rates(double* fp64_tflops, double* fp64_div_per_s, double* fp32_t
 
 /* Diagnostics: the FAST-mode FP64 reciprocal, reciprocal square root and
  * square root (an FP32 hardware seed and one third-order Newton step; within
- * 1, 1 and 2 ulp) of n device doubles x, written to the device array out as
- * [1/x | 1/sqrt(x) | sqrt(x)] (3n doubles), for tests of their error bounds. */
+ * 1, 1 and 2 ulp) and the second-order reciprocal (relative error below
+ * 2^-41) of n device doubles x, written to the device array out as
+ * [1/x | 1/sqrt(x) | sqrt(x) | 1/x second order] (4n doubles), for tests of
+ * their error bounds. */
 int weno_fast_math_eval(const double* x, double* out, int64_t n, void* stream);
 
 #ifdef __cplusplus

@@ -5,9 +5,11 @@ correctly rounded divide and square root in the FAST kernels.
 
 The device results (through weno_fast_math_eval) are compared with the same
 functions evaluated in numpy's extended precision (at least 64 significant
-bits): within 1 ulp for 1/x and 1/sqrt(x), 2 ulp for sqrt(x), over mantissas
-and exponents spread across the fast range [2^-1000, 2^1000] and the edges of
-the mantissa interval.  Outside the fast range (zero, subnormals, huge values,
+bits): within 1 ulp for 1/x and 1/sqrt(x), 2 ulp for sqrt(x), and a relative
+error below 2^-41 for the second-order reciprocal (the WENO weight
+normalisations and the Euler-flux density pair), over mantissas and exponents
+spread across the fast range [2^-1000, 2^1000] and the edges of the mantissa
+interval.  Outside the fast range (zero, subnormals, huge values,
 infinities, NaN) and for negative square-root arguments the functions take
 CUDA's IEEE operations: 1/x and sqrt(x) then equal numpy's correctly rounded
 results bit for bit.
@@ -26,12 +28,12 @@ def _eval(x):
     from weno_ext import _lib
     L = _lib.load()
     xd = torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).cuda()
-    out = torch.empty(3 * x.size, dtype=torch.float64, device="cuda")
+    out = torch.empty(4 * x.size, dtype=torch.float64, device="cuda")
     _lib.check(L.weno_fast_math_eval(xd.data_ptr(), out.data_ptr(), x.size,
                                      torch.cuda.current_stream().cuda_stream), "fast_math_eval")
     torch.cuda.synchronize()
     o = out.cpu().numpy()
-    return o[:x.size], o[x.size:2 * x.size], o[2 * x.size:]
+    return o[:x.size], o[x.size:2 * x.size], o[2 * x.size:3 * x.size], o[3 * x.size:]
 
 
 def _ulp_err(got, true_ld):
@@ -60,7 +62,7 @@ def test_reciprocal_within_one_ulp():
     rng = np.random.default_rng(11)
     x = _fast_range_sample(rng, 60000)
     x = np.concatenate([x, -x[:20000]])
-    r, _, _ = _eval(x)
+    r, _, _, _ = _eval(x)
     true = np.longdouble(1) / x.astype(np.longdouble)
     err = _ulp_err(r, true)
     assert err.max() <= RCP_ULP, (err.max(), x[err.argmax()])
@@ -69,10 +71,21 @@ def test_reciprocal_within_one_ulp():
     assert np.mean(r == 1.0 / x) > 0.98
 
 
+def test_second_order_reciprocal_within_bound():
+    rng = np.random.default_rng(13)
+    x = _fast_range_sample(rng, 60000)
+    x = np.concatenate([x, -x[:20000]])
+    _, _, _, r2 = _eval(x)
+    xl = x.astype(np.longdouble)
+    rel = np.abs((r2.astype(np.longdouble) * xl - 1).astype(np.float64))
+    assert rel.max() < 2.0 ** -41, (rel.max(), x[rel.argmax()])
+    assert np.all(np.sign(r2) == np.sign(x))
+
+
 def test_rsqrt_and_sqrt_within_bounds():
     rng = np.random.default_rng(12)
     x = _fast_range_sample(rng, 60000)
-    _, rs, sq = _eval(x)
+    _, rs, sq, _ = _eval(x)
     xl = x.astype(np.longdouble)
     true_sqrt = np.sqrt(xl)
     e_rs = _ulp_err(rs, np.longdouble(1) / true_sqrt)
@@ -86,11 +99,12 @@ def test_outside_fast_range_takes_ieee():
     huge = np.ldexp(1.0, 1001)
     x = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, 1e-310, -1e-310, tiny, tiny * 1.7, huge, huge * 1.3,
                   1.7e308, -1.7e308, np.ldexp(1.0, -1022), np.ldexp(1.5, 1023)])
-    r, rs, sq = _eval(x)
+    r, rs, sq, r2 = _eval(x)
     with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
         want_r = 1.0 / x
         want_sq = np.sqrt(x)
     assert np.array_equal(r, want_r, equal_nan=True)
+    assert np.array_equal(r2, want_r, equal_nan=True)
     assert np.array_equal(sq, want_sq, equal_nan=True)
     # CUDA's rsqrt: the limits exactly, finite values within 2 ulp
     assert np.isposinf(rs[0]) and np.isneginf(rs[1]) and rs[2] == 0.0 and np.isnan(rs[3]) and np.isnan(rs[4])
@@ -99,5 +113,5 @@ def test_outside_fast_range_takes_ieee():
     true = np.longdouble(1) / np.sqrt(x[pos].astype(np.longdouble))
     assert _ulp_err(rs[pos], true).max() <= 2.0
     # negative arguments of the square roots: NaN
-    _, rs_n, sq_n = _eval(np.array([-1.0, -3.5e10, -1e-300]))
+    _, rs_n, sq_n, _ = _eval(np.array([-1.0, -3.5e10, -1e-300]))
     assert np.all(np.isnan(rs_n)) and np.all(np.isnan(sq_n))

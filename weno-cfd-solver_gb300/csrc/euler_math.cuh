@@ -172,8 +172,9 @@ __device__ __forceinline__ void euler_flux(const T q[4], T gamma, T f[4], T rinv
 }
 
 // Two Euler fluxes (utils.rs:74-109).  FAST native double shares one division
-// between the two densities: 1/(rho_a rho_b), whose product stays in range for
-// any clamped density below 1e150 (otherwise two divisions).
+// between the two densities: 1/(rho_a rho_b) (f64fast::rcp2, relative error
+// below 2^-41), whose product stays in range for any clamped density below
+// 1e150 (otherwise two divisions).
 template <class T, bool FAST, bool Y>
 __device__ __forceinline__ void euler_flux_pair(const T qa[4], const T qb[4], T gamma, T fa[4], T fb[4]) {
   if constexpr (FAST && is_native_f64<T>) {
@@ -181,7 +182,7 @@ __device__ __forceinline__ void euler_flux_pair(const T qa[4], const T qb[4], T 
     const T prod = ra * rb;
     T ia, ib;
     if (lt_bound<T, FAST>(prod, T(1e300))) {
-      const T inv = f64fast::rcp(prod);
+      const T inv = f64fast::rcp2(prod);
       ia = rb * inv;
       ib = ra * inv;
     } else {
@@ -326,7 +327,7 @@ __device__ __forceinline__ void div_pair(double a, double b, double c, double d,
   const double bd = b * d;
   const int e = (__double2hiint(bd) >> 20) & 0x7ff;
   if (e > 64 && e < 1983) {
-    const double inv = f64fast::rcp(bd * k);
+    const double inv = f64fast::rcp2(bd * k);  // scales the slopes only
     x = fma(a * d, inv, x0);
     y = fma(c * b, inv, y0);
   } else {
@@ -442,7 +443,7 @@ __device__ __forceinline__ void gq_weights(T q2, T h0, T h1, T h2, T f0, T f1, T
     constexpr double r0 = kGqA0 / kGqA1, r2 = kGqA2 / kGqA1;
     const double u0 = P0 * h0, u1 = P1 * h1, u2 = P2 * h2;
     const double sa = fma(r0, P0, fma(r2, P2, P1)), sb = fma(r2, P0, fma(r0, P2, P1));
-    const double t = S * f64fast::rcp(sa * sb);
+    const double t = S * f64fast::rcp2(sa * sb);  // scales the weighted slopes only
     // point a: candidates (q2 + S h0, q2 - S h1, q2 - S h2); point b: the mirror
     ra = fma(r0, u0, fma(-r2, u2, -u1)) * (sb * t) + q2;
     rb = fma(r0, u2, fma(-r2, u0, u1)) * (sa * t) + q2;

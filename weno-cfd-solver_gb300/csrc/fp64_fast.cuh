@@ -23,6 +23,12 @@
 // root (x times its reciprocal square root) within 2 ulp.  Arguments whose
 // exponent lies outside [-1000, 1000] (zero, subnormals, infinities, NaN) and
 // negative arguments of the square roots take CUDA's IEEE operations.
+//
+// rcp2 stops the series after e (Newton's step, two FP64 operations): relative
+// error below 2^-41 (the seed's error squared).  It serves quotients whose
+// relative error only scales a small correction -- the normalisation of the
+// WENO weights, which multiplies the weighted slope added to a centre value,
+// and the shared 1/(rho_a rho_b) of two Euler fluxes.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -70,6 +76,16 @@ __device__ __forceinline__ double rcp_core(int hi, int lo) {
   return __hiloint2double(yh | (hi & (int)0x80000000), __double2loint(y));
 }
 
+// The same with the series truncated after e.
+__device__ __forceinline__ double rcp2_core(int hi, int lo) {
+  const int ex = biased_exp(hi);
+  const double m = __hiloint2double((hi & 0x000fffff) | 0x3ff00000, lo);
+  const double y0 = widen(rcp_approx(narrow(hi, lo, 127u)));
+  const double y = fma(y0, fma(-m, y0, 1.0), y0);  // in [0.5, 1]
+  const int yh = __double2hiint(y) - (ex - 1023) * (1 << 20);
+  return __hiloint2double(yh | (hi & (int)0x80000000), __double2loint(y));
+}
+
 // 1/sqrt(x) for positive x with biased exponent in [kExpLo, kExpHi].
 __device__ __forceinline__ double rsqrt_core(int hi, int lo) {
   const int e2 = biased_exp(hi) - 1023;
@@ -87,6 +103,13 @@ __device__ __forceinline__ double rcp(double x) {
   const int ex = biased_exp(hi);
   if (ex < kExpLo || ex > kExpHi) return 1.0 / x;
   return rcp_core(hi, lo);
+}
+
+__device__ __forceinline__ double rcp2(double x) {
+  const int hi = __double2hiint(x), lo = __double2loint(x);
+  const int ex = biased_exp(hi);
+  if (ex < kExpLo || ex > kExpHi) return 1.0 / x;
+  return rcp2_core(hi, lo);
 }
 
 __device__ __forceinline__ double rsqrt(double x) {

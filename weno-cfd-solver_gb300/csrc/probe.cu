@@ -35,6 +35,7 @@ __global__ void k_fast_math(const double* x, double* out, int64_t n) {
   out[i] = weno::f64fast::rcp(v);
   out[n + i] = weno::f64fast::rsqrt(v);
   out[2 * n + i] = weno::f64fast::sqrt(v);
+  out[3 * n + i] = weno::f64fast::rcp2(v);
 }
 
 template <class F>
