@@ -67,9 +67,9 @@ __device__ __forceinline__ T vmin(T a, T b) { return fmin(a, b); }
 // FP64 compares and min/max at the FP64 rate).  A NaN x with the sign bit clear
 // passes through where fmax would return the bound; NaN propagates through
 // the neighbouring arithmetic either way.  Used by the fluxes and the Riemann
-// solvers (pass 2); the pass-1 Roe average and limiter keep the FP64 forms,
-// with which the characteristic pass 1 compiles to 112 registers (4 CTAs per
-// SM), measured faster than the 92-register (5 CTA) build the integer forms give.
+// solvers (pass 2); the pass-1 Roe average and limiter keep the FP64 forms:
+// there the integer forms measured 1.6 % slower, at 5 resident CTAs per SM
+// and equally when held to the FP64 build's 4.
 template <class T, bool FAST>
 __device__ __forceinline__ T cmax(T x, T c) {
   if constexpr (FAST && is_native_f64<T>) return __double_as_longlong(x) > __double_as_longlong(c) ? x : c;
