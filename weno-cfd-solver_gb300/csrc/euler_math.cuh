@@ -58,6 +58,13 @@ template <class T>
 __device__ __forceinline__ T vmax(T a, T b) { return fmax(a, b); }
 template <class T>
 __device__ __forceinline__ T vmin(T a, T b) { return fmin(a, b); }
+// a*b + c as one FMA where the type has one (the FAST forms that must round
+// the same way in two kernels spell it out).
+template <class T>
+__device__ __forceinline__ T mul_add(T a, T b, T c) {
+  if constexpr (is_native_f64<T> || is_f32<T>) return fma(a, b, c);
+  else return a * b + c;
+}
 
 // Clamps and tests against a non-negative bound.  FAST native double reads the
 // operands' bits as signed 64-bit integers: for non-negative doubles that order
@@ -509,36 +516,61 @@ __device__ __forceinline__ void weno5_gq_pair(T q0, T q1, T q2, T q3, T q4, T& r
 // ---------------------------------------------------------------------------
 // Characteristic projection (weno.rs:13-205)
 // ---------------------------------------------------------------------------
-// Roe average of two conserved cells, weno.rs:13-52.
-// FAST also returns 1/c_roe and 1/rho_roe (ic, irho) for the eigenvectors:
-// with r = 1/sqrt(rho) per side, sqrt(rho) = rho r, 1/rho = r r, sqrt(rho) u =
-// m r, and 1/rho_roe = r_l r_r, so the average costs two reciprocal square
-// roots, one divide and one more reciprocal square root for c.
+// FAST Roe-average inputs of one cell: with r = 1/sqrt(rho) (one reciprocal
+// square root), sqrt(rho) = rho r, 1/rho = r r, sqrt(rho) u = m r and
+// sqrt(rho) v = n r; E + p with the clamped pressure.
+template <class T>
+struct RoeSide {
+  T sq, r, i, a, b, ep;  // sqrt(rho), 1/sqrt(rho), 1/rho, m r, n r, E + p
+};
+
+template <class T>
+__device__ __forceinline__ RoeSide<T> roe_side(const T u[4], T gamma) {
+  RoeSide<T> s;
+  const T rho = vmax(u[0], T(kEps));
+  s.r = frsqrt(rho);
+  s.sq = rho * s.r;
+  s.i = s.r * s.r;
+  // kinetic energy (m^2 + n^2) / (2 rho): the velocities themselves are not needed
+  const T p = vmax((gamma - T(1.0)) * (u[3] - T(0.5) * ((u[1] * u[1] + u[2] * u[2]) * s.i)), T(kEps));
+  s.a = u[1] * s.r;
+  s.b = u[2] * s.r;
+  s.ep = u[3] + p;
+  return s;
+}
+
+// Roe average of the face between sides L and R (weno.rs:13-52), FAST: m_l,
+// n_l are the left cell's momenta.  Also returns 1/c_roe and 1/rho_roe (ic,
+// irho) for the eigenvectors; 1/rho_roe = r_l r_r.
+template <class T>
+__device__ __forceinline__ void roe_face(const RoeSide<T>& L, const RoeSide<T>& R, T m_l, T n_l, T gamma,
+                                         T& rho_roe, T& u_roe, T& v_roe, T& h_roe, T& c_roe, T& ic, T& irho) {
+  const T id = qrcp<T, true>(L.sq + R.sq);
+  u_roe = mul_add(m_l, L.r, R.a) * id;
+  v_roe = mul_add(n_l, L.r, R.b) * id;
+  h_roe = mul_add(L.ep, L.r, R.ep * R.r) * id;
+  const T kin = T(0.5) * (u_roe * u_roe + v_roe * v_roe);
+  const T c2 = vmax((gamma - T(1.0)) * (h_roe - kin), T(kEps) * vmax(L.i, R.i));
+  ic = frsqrt(c2);
+  c_roe = c2 * ic;
+  rho_roe = L.sq * R.sq;
+  irho = L.r * R.r;
+}
+
+// Roe average of two conserved cells, weno.rs:13-52 (FAST: roe_side and
+// roe_face, two reciprocal square roots, one divide and one more reciprocal
+// square root for c).
 template <class T, bool FAST>
 __device__ __forceinline__ void roe_avg(const T ul[4], const T ur[4], T gamma, T& rho_roe, T& u_roe, T& v_roe,
                                         T& h_roe, T& c_roe, T& ic, T& irho) {
-  const T rho_l = vmax(ul[0], T(kEps));
-  const T rho_r = vmax(ur[0], T(kEps));
   if constexpr (FAST) {
-    const T rl = frsqrt(rho_l), rr = frsqrt(rho_r);
-    const T sqrt_l = rho_l * rl, sqrt_r = rho_r * rr;
-    const T il = rl * rl, ir = rr * rr;
-    // kinetic energy (m^2 + n^2) / (2 rho): the velocities themselves are not needed
-    const T p_l = vmax((gamma - T(1.0)) * (ul[3] - T(0.5) * ((ul[1] * ul[1] + ul[2] * ul[2]) * il)), T(kEps));
-    const T p_r = vmax((gamma - T(1.0)) * (ur[3] - T(0.5) * ((ur[1] * ur[1] + ur[2] * ur[2]) * ir)), T(kEps));
-    const T id = qrcp<T, FAST>(sqrt_l + sqrt_r);
-    u_roe = (ul[1] * rl + ur[1] * rr) * id;
-    v_roe = (ul[2] * rl + ur[2] * rr) * id;
-    h_roe = ((ul[3] + p_l) * rl + (ur[3] + p_r) * rr) * id;
-    const T kin = T(0.5) * (u_roe * u_roe + v_roe * v_roe);
-    const T c2 = vmax((gamma - T(1.0)) * (h_roe - kin), T(kEps) * vmax(il, ir));
-    ic = frsqrt(c2);
-    c_roe = c2 * ic;
-    rho_roe = sqrt_l * sqrt_r;
-    irho = rl * rr;
+    roe_face(roe_side(ul, gamma), roe_side(ur, gamma), ul[1], ul[2], gamma, rho_roe, u_roe, v_roe, h_roe, c_roe, ic,
+             irho);
   } else {
     (void)ic;
     (void)irho;
+    const T rho_l = vmax(ul[0], T(kEps));
+    const T rho_r = vmax(ur[0], T(kEps));
     const T sqrt_l = sqrt(rho_l);
     const T sqrt_r = sqrt(rho_r);
     const T denom = sqrt_l + sqrt_r;
