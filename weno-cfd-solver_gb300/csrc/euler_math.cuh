@@ -375,7 +375,8 @@ __device__ __forceinline__ T weno5_right(T u1, T u2, T u3, T u4, T u5, T weps) {
 }
 
 // weno5_left and weno5_right of one field at one face (the right stencil is
-// the left one shifted by a cell), FAST native double with one shared divide.
+// the left one shifted by a cell), FAST: native double shares one divide
+// between the two; float and df64 take reciprocal weights.
 template <class T>
 __device__ __forceinline__ void weno5_lr_fast(T u0, T u1, T u2, T u3, T u4, T u5, T weps, T& left, T& right) {
   // first differences d_m = u_{m+1} - u_m, second differences D_m = d_m - d_{m-1}

@@ -10,8 +10,9 @@
 // Residual pipeline for one direction (x shown; y swaps the roles of i and j):
 //   pass1   (m-5) x n   faces x columns : normal WENO5 (char or cons) -> q_l, q_r
 //   pass2   (m-5) x (n-6) faces        : transverse 2-point Gauss WENO of q_l,
-//           q_r, Euler fluxes of the four Gauss states, face averages, then the
-//           HLLE flux, or HLLC + HLLE + mean pressure for the sensor blend
+//           q_r, Euler fluxes of the four Gauss states, face averages (the FAST
+//           HLLE takes their doubles, the Gauss-point sums), then the HLLE
+//           flux, or HLLC + HLLE + mean pressure for the sensor blend
 //   blend   (sensor blend only)        : pressure-gradient weight, F
 //   residual (m-6) x (n-6) cells       : -(dF/dx + dG/dy), optionally fused
 //           with the SSP-RK3 stage combination.
