@@ -317,13 +317,24 @@ __device__ __forceinline__ T weno_combine(T e0, T e1, T e2, T d0, T d1, T d2, T 
 // a caller can share one divide between two reconstructions; the (eps+b_k)
 // are first brought into a safe range (weno_range), so the products neither
 // overflow nor lose the dominant weight whatever the magnitude of the values.
-__device__ __forceinline__ void weno_nd(double e0, double e1, double e2, double d0, double d1, double d2, double p0,
-                                        double p1, double p2, double scale, double& num, double& den) {
+__device__ __forceinline__ void weno_nd_products(double e0, double e1, double e2, double& P0, double& P1,
+                                                 double& P2) {
   weno_range(e0, e1, e2);
   const double s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
-  const double c0 = d0 * (s1 * s2), c1 = d1 * (s0 * s2), c2 = d2 * (s0 * s1);
-  num = c0 * p0 + c1 * p1 + c2 * p2;
-  den = (c0 + c1 + c2) * scale;
+  P0 = s1 * s2;
+  P1 = s0 * s2;
+  P2 = s0 * s1;
+}
+// Numerator and denominator of the weighted slope from the products, linear
+// weights (3, 6, 1) (the reference's 0.3, 0.6, 0.1 scaled by 10), each
+// operation spelled out: two reconstructions that share the products (the
+// same three stencils seen from both sides of a cell) round exactly as two
+// separate evaluations would.
+__device__ __forceinline__ void weno_nd_combine(double P0, double P1, double P2, double g0, double g1, double g2,
+                                                double& num, double& den) {
+  const double c0 = 3.0 * P0, c1 = 6.0 * P1;
+  num = fma(P2, g2, fma(c1, g1, c0 * g0));
+  den = (c0 + c1) + P2;
 }
 
 // x = x0 + a/(k b) and y = y0 + c/(k d) with one divide, 1/(k b d), when b d is
@@ -406,14 +417,57 @@ __device__ __forceinline__ void weno5_lr_fast(T u0, T u1, T u2, T u3, T u4, T u5
   if constexpr (is_native_f64<T>) {
     // linear weights scaled by 10 -- (3, 6, 1) -- and the 1/6 of the candidate
     // polynomials applied once to the shared divide
-    double nl, dl, nr, dr;
-    weno_nd(el0, el1, el2, 3.0, 6.0, 1.0, gl0, gl1, gl2, 1.0, nl, dl);
-    weno_nd(er2, er1, er0, 3.0, 6.0, 1.0, gr2, gr1, gr0, 1.0, nr, dr);
+    double P0, P1, P2, nl, dl, nr, dr;
+    weno_nd_products(el0, el1, el2, P0, P1, P2);
+    weno_nd_combine(P0, P1, P2, gl0, gl1, gl2, nl, dl);
+    weno_nd_products(er2, er1, er0, P0, P1, P2);
+    weno_nd_combine(P0, P1, P2, gr2, gr1, gr0, nr, dr);
     div_pair(nl, dl, nr, dr, left, right, 6.0, u2, u3);
   } else {
     left = u2 + weno_combine<T, true>(el0, el1, el2, T(0.3), T(0.6), T(0.1), gl0, gl1, gl2, T(6.0));
     right = u3 + weno_combine<T, true>(er2, er1, er0, T(0.3), T(0.6), T(0.1), gr2, gr1, gr0, T(6.0));
   }
+}
+
+// weno5_lr_fast of two neighbouring faces of one field (A between u2 and u3,
+// B between u3 and u4; FAST native double), sharing what the two faces have in
+// common: the differences, and -- since A's right state and B's left state are
+// both reconstructions about cell u3 from the stencils 1-3, 2-4, 3-5 -- their
+// indicators and weight products.  Every shared value is computed with the
+// operations weno5_lr_fast performs for each face on its own, so A and B get
+// the bits of two separate calls (the component-wise pass 1 of the FAST
+// double solver).
+__device__ __forceinline__ void weno5_lr_fast_two(double u0, double u1, double u2, double u3, double u4, double u5,
+                                                  double u6, double weps, double& lA, double& rA, double& lB,
+                                                  double& rB) {
+  const double d0 = u1 - u0, d1 = u2 - u1, d2 = u3 - u2, d3 = u4 - u3, d4 = u5 - u4, d5 = u6 - u5;
+  const double D1 = d1 - d0, D2 = d2 - d1, D3 = d3 - d2, D4 = d4 - d3, D5 = d5 - d4;
+  const double w4 = 4.0 * weps;
+  const double C1 = kC43 * D1 * D1 + w4, C2 = kC43 * D2 * D2 + w4, C3 = kC43 * D3 * D3 + w4,
+               C4 = kC43 * D4 * D4 + w4, C5 = kC43 * D5 * D5 + w4;
+  // face A: as weno5_lr_fast(u0..u5)
+  const double sl0 = d3 - 3.0 * d2, sl1 = d1 + d2, sl2 = 3.0 * d1 - d0;
+  const double sr0 = d4 - 3.0 * d3, sr1 = d2 + d3, sr2 = 3.0 * d2 - d1;
+  const double el0 = sl0 * sl0 + C3, el1 = sl1 * sl1 + C2, el2 = sl2 * sl2 + C1;
+  const double er0 = sr0 * sr0 + C4, er1 = sr1 * sr1 + C3, er2 = sr2 * sr2 + C2;
+  const double gl0 = d2 - sl0, gl1 = sl1 + d2, gl2 = 2.0 * sl2 - d1;
+  const double gr2 = -d2 - sr2, gr1 = -d2 - sr1, gr0 = 2.0 * sr0 + d3;
+  // face B: as weno5_lr_fast(u1..u6); its left stencils and indicators are A's right ones
+  const double tr0 = d5 - 3.0 * d4, tr1 = d3 + d4, tr2 = 3.0 * d3 - d2;
+  const double fr0 = tr0 * tr0 + C5, fr1 = tr1 * tr1 + C4, fr2 = tr2 * tr2 + C3;
+  const double hl0 = d3 - sr0, hl1 = sr1 + d3, hl2 = 2.0 * sr2 - d2;
+  const double hr2 = -d3 - tr2, hr1 = -d3 - tr1, hr0 = 2.0 * tr0 + d4;
+  double P0, P1, P2, nl, dl, nr, dr;
+  weno_nd_products(el0, el1, el2, P0, P1, P2);
+  weno_nd_combine(P0, P1, P2, gl0, gl1, gl2, nl, dl);
+  weno_nd_products(er2, er1, er0, P0, P1, P2);
+  weno_nd_combine(P0, P1, P2, gr2, gr1, gr0, nr, dr);
+  div_pair(nl, dl, nr, dr, lA, rA, 6.0, u2, u3);
+  // B's left from the same products in the other order (products commute)
+  weno_nd_combine(P2, P1, P0, hl0, hl1, hl2, nl, dl);
+  weno_nd_products(fr2, fr1, fr0, P0, P1, P2);
+  weno_nd_combine(P0, P1, P2, hr2, hr1, hr0, nr, dr);
+  div_pair(nl, dl, nr, dr, lB, rB, 6.0, u3, u4);
 }
 
 // FAST float: the four fields' left/right reconstructions as two packed pairs

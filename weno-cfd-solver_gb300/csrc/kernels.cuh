@@ -90,6 +90,38 @@ __global__ void __launch_bounds__(128) k_pass1(CView<T> u, int64_t rows, int64_t
   }
 }
 
+// Component-wise pass 1, FAST double: two neighbouring faces per thread along
+// the sweep (rows for x, columns for y), whose seven cells and shared
+// reconstructions about the middle cell serve both (weno5_lr_fast_two; the
+// same bits as one face per thread).
+template <bool Y>
+__global__ void __launch_bounds__(128) k_pass1_cons2(CView<double> u, int64_t rows, int64_t cols,
+                                                      Planes<double> PL, Planes<double> PR, double weps) {
+  int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t row = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
+  if constexpr (Y) col *= 2;
+  else row *= 2;
+  if (row >= rows || col >= cols) return;
+  const bool two = Y ? (col + 1 < cols) : (row + 1 < rows);
+  const int64_t rowB = Y ? row : row + 1, colB = Y ? col + 1 : col;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    double v[7];
+#pragma unroll
+    for (int s = 0; s < 6; ++s) v[s] = Y ? u.at(row, col + s, k) : u.at(row + s, col, k);
+    // the seventh cell exists only when face B does
+    v[6] = two ? (Y ? u.at(row, col + 6, k) : u.at(row + 6, col, k)) : v[5];
+    double lA, rA, lB, rB;
+    weno5_lr_fast_two(v[0], v[1], v[2], v[3], v[4], v[5], v[6], weps, lA, rA, lB, rB);
+    PL.at(k, row, col) = lA;
+    PR.at(k, row, col) = rA;
+    if (two) {
+      PL.at(k, rowB, colB) = lB;
+      PR.at(k, rowB, colB) = rB;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Pass 2 (weno.rs:460-501 / :587-631) + Riemann solver (riemann.rs)
 // ---------------------------------------------------------------------------

@@ -40,6 +40,14 @@ cudaError_t Launch<T, FAST>::pass1(HostView u, int64_t rows, int64_t cols, doubl
   const dim3 g = grid2d(rows, cols, kBlk);
   auto U = cview<T>(u);
   auto L = planes<T>(PL), R = planes<T>(PR);
+  if constexpr (FAST && std::is_same<T, double>::value) {
+    if (!chr) {  // component-wise: two faces per thread along the sweep
+      const dim3 g2 = ydir ? grid2d(rows, (cols + 1) / 2, kBlk) : grid2d((rows + 1) / 2, cols, kBlk);
+      if (!ydir) k_pass1_cons2<false><<<g2, kBlk, 0, st>>>(U, rows, cols, L, R, weps);
+      else k_pass1_cons2<true><<<g2, kBlk, 0, st>>>(U, rows, cols, L, R, weps);
+      return cudaGetLastError();
+    }
+  }
   if (!ydir && chr) k_pass1<T, FAST, false, true><<<g, kBlk, 0, st>>>(U, rows, cols, (T)gamma, L, R, (T)weps);
   else if (!ydir) k_pass1<T, FAST, false, false><<<g, kBlk, 0, st>>>(U, rows, cols, (T)gamma, L, R, (T)weps);
   else if (chr) k_pass1<T, FAST, true, true><<<g, kBlk, 0, st>>>(U, rows, cols, (T)gamma, L, R, (T)weps);
