@@ -13,10 +13,12 @@
  * Arithmetic policy (`mode`):
  *   WENO_EXACT  the reference's operation order with no FMA contraction: the
  *               doubles are bit-identical to the Rust core's.
- *   WENO_FAST   the same scheme with fewer FP64 divides and FMA contraction,
- *               and reciprocals / square roots within 1-2 ulp (seeded Newton
- *               steps, see weno_fast_math_eval); agrees with WENO_EXACT to
- *               rounding.
+ *   WENO_FAST   the same scheme with fewer FP64 operations and FMA
+ *               contraction: reciprocals / square roots within 1-2 ulp
+ *               (seeded Newton steps, see weno_fast_math_eval), the WENO
+ *               weight normalisations within 2^-41; agrees with WENO_EXACT
+ *               to rounding (about 1e-16 relative L1 on a step, within 1e-10
+ *               over multi-step runs).
  *
  * Return value: WENO_OK (0) or an error code; weno_last_error() describes the
  * last error of the calling thread.

@@ -18,7 +18,8 @@ arrays need at least 4 channels (the reference asserts c >= 4, weno.rs:371).
 
 Arithmetic: ``set_mode("exact")`` (default) reproduces the Rust core's IEEE
 doubles bit for bit; ``set_mode("fast")`` (or WENO_EXT_MODE=fast) uses the
-reformulated kernels with fewer FP64 divides, equal to rounding.
+reformulated kernels with fewer FP64 operations, equal to rounding (about
+1e-16 relative L1 on a step, within 1e-10 over multi-step runs).
 """
 
 from __future__ import annotations
