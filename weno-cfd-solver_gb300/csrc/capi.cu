@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/weno_gb300.h"
+#include "ctx_id.h"
 #include <nvtx3/nvToolsExt.h>
 
 #include "df64.cuh"
@@ -302,6 +303,7 @@ struct HostCache {
   void* ws = nullptr;
   size_t ws_bytes = 0;
   cudaStream_t st = nullptr;
+  unsigned long long ctx = 0;  // context that owns the buffers and the stream
 };
 std::mutex g_host_mu;
 std::map<int, HostCache> g_host_cache;
@@ -330,7 +332,14 @@ extern "C" int weno_l_local_host(const double* u, int64_t m, int64_t n, int64_t 
   WENO_CK(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(g_host_mu);
   HostCache& hc = g_host_cache[dev];
-  if (!hc.st) WENO_CK(cudaStreamCreateWithFlags(&hc.st, cudaStreamNonBlocking));
+  // buffers of a context that has since been destroyed (cudaDeviceReset) are
+  // dropped, not freed: they went with it
+  const unsigned long long ctx = weno::current_context_id();
+  if (hc.st && ctx != 0 && hc.ctx != 0 && ctx != hc.ctx) hc = HostCache();
+  if (!hc.st) {
+    WENO_CK(cudaStreamCreateWithFlags(&hc.st, cudaStreamNonBlocking));
+    hc.ctx = weno::current_context_id();
+  }
   const size_t in_bytes = (size_t)(m * n * c) * sizeof(double);
   const size_t out_bytes = (size_t)((m - 6) * (n - 6) * 4) * sizeof(double);
   ResidualLayout Lo(m, n, force_hlle != 0, sizeof(double));

@@ -31,6 +31,7 @@
 #include <mutex>
 
 #include "../../include/weno_gb300.h"
+#include "ctx_id.h"
 #include "errors.h"
 
 namespace {
@@ -43,36 +44,6 @@ static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 std::mutex g_mu;
 void* g_scratch_addr[kMaxDevices] = {};
 unsigned long long g_scratch_ctx[kMaxDevices] = {};
-
-// The current context's unique id (cuCtxGetId), fetched through the runtime so
-// the library need not link the driver library; 0 if the driver lacks it, in
-// which case the address is looked up on every call.
-using CtxGetCurrentFn = CUresult (*)(CUcontext*);
-using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
-
-unsigned long long current_context_id() {
-  static CtxGetCurrentFn get_current = [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      p = nullptr;
-    return reinterpret_cast<CtxGetCurrentFn>(p);
-  }();
-  static CtxGetIdFn get_id = [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      p = nullptr;
-    return reinterpret_cast<CtxGetIdFn>(p);
-  }();
-  if (!get_current || !get_id) return 0;
-  CUcontext ctx = nullptr;
-  unsigned long long id = 0;
-  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
-  return id;
-}
 
 }  // namespace
 
@@ -93,7 +64,7 @@ extern "C" int weno_l_local_noalloc(const double* u, int64_t m, int64_t n, int64
   if (dev < 0 || dev >= kMaxDevices) return weno::set_last_error(WENO_ERR_ARG, "l_local_noalloc: device index too large");
   // 0 when no context is current yet: the lookup below creates the device's
   // primary context, and the id is read again after it.
-  const unsigned long long ctx = current_context_id();
+  const unsigned long long ctx = weno::current_context_id();
   void* ptr = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -105,7 +76,7 @@ extern "C" int weno_l_local_noalloc(const double* u, int64_t m, int64_t n, int64
         return weno::set_last_error(WENO_ERR_CUDA, msg);
       }
       g_scratch_addr[dev] = ptr;
-      g_scratch_ctx[dev] = current_context_id();
+      g_scratch_ctx[dev] = weno::current_context_id();
     }
     ptr = g_scratch_addr[dev];
   }
