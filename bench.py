@@ -945,8 +945,9 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(nx, int(os.environ.get("WENO_CPU_STRIP", "32")), os.cpu_count() or 1)
     if rank == 0 and world == 1 and args.precision == "f64" and (nx, ny) == (4096, 4096):
-        # The other figures BASELINE's metric names, on the same box in the same run
-        # (the default workload only: smaller --nx/--ny runs are profiling cases).
+        # The headline metric's other figures (the drop-in call rate, the batched FP32
+        # rate, the serving p50/p99), on the same box in the same run (the default
+        # workload only: smaller --nx/--ny runs are profiling cases).
         torch.cuda.empty_cache()
         if not args.no_dropin:
             line["e2e_dropin"] = dropin_host_leg(nx, ny)
